@@ -1,0 +1,202 @@
+/*
+ * qdfn.h -- C ABI of libqdfn.so, the GB300 (sm_103a) implementation of the
+ * Quake-DFN earthquake-cycle hot path.
+ *
+ * Conventions
+ *   - Every function returns int: 0 (QDFN_OK) or a negative QDFN_ERR_* code;
+ *     nothing throws across the ABI.  qdfn_last_error() gives the message of the
+ *     last failure on the calling thread.
+ *   - Functions without a _dev suffix take HOST pointers owned by the caller;
+ *     the data are copied during the call.  _dev functions take DEVICE pointers
+ *     and a cudaStream_t passed as void*.
+ *   - Indices are 0-based.  A matrix argument has a `layout`:
+ *       QDFN_LAYOUT_ROW (0): K[r * ld + s]   (row = receiver, C order)
+ *       QDFN_LAYOUT_COL (1): K[s * ld + r]   (Julia's column-major K[recv, src])
+ *   - One context is driven by one host thread at a time; contexts are
+ *     independent of each other.
+ *   - Angles are in degrees; lengths in metres; stresses in Pa.
+ *
+ * Reference interfaces replaced (paths inside limkjae/Quake-DFN):
+ *   assembly   scripts/Functions_BuildInputFile.jl:386  StiffnessMatrix_ByParts_Calculation_Rec
+ *              scripts/Functions_BuildInputFile.jl:516  BuildMatrixByParts_Even_Rec
+ *              scripts/Functions_BuildInputFile.jl:551  StiffnessMatrix_ByParts_Calculation_Tri
+ *              scripts/Functions_BuildInputFile.jl:599  BuildMatrixByParts_Even_Tri
+ *              scripts/Functions_OKADA3D.jl:464         Okada_DC3D_Vector
+ *              scripts/Functions_TDstressHS.jl:2        TDstressHS
+ *   simulation scripts/Functions_RSFDFN3DMain_D.jl:2     main   (dense)
+ *              scripts/Functions_RSFDFN3DMain_H.jl:2     main_H (H-matrix)
+ *              scripts/Functions_Solvers.jl:334          SolveOneTimeStep (+ :26, :185, :2, :465)
+ *              scripts/Functions_Hmatrix.jl:631          HmatSolver_Pararllel
+ */
+#ifndef QDFN_H
+#define QDFN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QDFN_OK 0
+#define QDFN_ERR_INVALID -1      /* bad argument */
+#define QDFN_ERR_CUDA -2         /* CUDA runtime error */
+#define QDFN_ERR_NOMEM -3        /* device allocation failed */
+#define QDFN_ERR_STATE -4        /* call out of order (e.g. run before set_dense) */
+#define QDFN_ERR_DOMAIN -10      /* log/sqrt of a negative number (Julia DomainError) */
+#define QDFN_ERR_EMPTY -11       /* minimum over an empty set in the time-step control */
+#define QDFN_ERR_RETRIES -12     /* retry loop of one step passed its cap */
+#define QDFN_ERR_NO_CONVERGE -13 /* per-patch iteration passed its cap */
+#define QDFN_ERR_TIMEOUT -14     /* device-side deadline passed (kernel returned early) */
+#define QDFN_ERR_HALF_SPACE -15  /* triangle vertex or receiver above the free surface */
+
+#define QDFN_LAYOUT_ROW 0
+#define QDFN_LAYOUT_COL 1
+
+/* storage precision of the elastic operator */
+#define QDFN_FP64 0
+#define QDFN_FP32 1
+#define QDFN_BF16X2 2   /* value = hi + lo, both bfloat16 (4 bytes per entry) */
+
+/* ---- library ------------------------------------------------------------ */
+/* Version string of the library. */
+const char* qdfn_version(void);
+/* Message for a status code. */
+const char* qdfn_status_string(int status);
+/* Copies the last error message of the calling thread into buf (NUL-terminated). */
+int qdfn_last_error(char* buf, size_t n);
+
+/* ---- stiffness assembly -------------------------------------------------- */
+/* Rectangular patches, Okada (1992) DC3D.  src/recv are n x 8 row-major records
+ *   {centre_x, centre_y, centre_z (depth, positive down), strike length,
+ *    dip length, strike, dip, rake}.
+ * Ks, Kn: n_recv x n_src in `layout` with leading dimension n_recv (COL) or
+ * n_src (ROW).  Replaces StiffnessMatrix_ByParts_Calculation_Rec
+ * (Functions_BuildInputFile.jl:386-512) and its part driver (:516-548). */
+int qdfn_assemble_rect(int64_t n_src, const double* src, int64_t n_recv, const double* recv,
+                       double shear_modulus, double poisson, double* Ks, double* Kn, int layout);
+/* Device-pointer form; ld is the leading dimension of Ks/Kn. */
+int qdfn_assemble_rect_dev(int64_t n_src, const double* src, int64_t n_recv, const double* recv,
+                           double shear_modulus, double poisson, double* Ks, double* Kn,
+                           int64_t ld, int layout, void* stream);
+
+/* Triangular patches, Nikkhoo & Walter (2015) TDstressHS.
+ * P1,P2,P3: n_src x 3 vertices (z <= 0, up positive, already reordered by
+ * RotVerts_UnitVectors), rake: n_src; centre, nhat, shat: n_recv x 3 receiver
+ * centroids, unit normals and unit slip vectors.  Replaces
+ * StiffnessMatrix_ByParts_Calculation_Tri (Functions_BuildInputFile.jl:551-594). */
+int qdfn_assemble_tri(int64_t n_src, const double* P1, const double* P2, const double* P3,
+                      const double* rake, int64_t n_recv, const double* centre, const double* nhat,
+                      const double* shat, double shear_modulus, double poisson, double* Ks,
+                      double* Kn, int layout);
+int qdfn_assemble_tri_dev(int64_t n_src, const double* P1, const double* P2, const double* P3,
+                          const double* rake, int64_t n_recv, const double* centre,
+                          const double* nhat, const double* shat, double shear_modulus,
+                          double poisson, double* Ks, double* Kn, int64_t ld, int layout,
+                          void* stream);
+
+/* ---- cycle simulation ------------------------------------------------------ */
+typedef struct qdfn_ctx qdfn_ctx;
+
+/* Problem description.  Per-patch arrays have length n_inst * N (instance-major:
+ * instance k owns [k*N, (k+1)*N)); instances share the elastic operator and the
+ * loading-fault count (friction draws on one geometry).  Fields follow the
+ * positional arguments of main() (Functions_RSFDFN3DMain_D.jl:2-8). */
+typedef struct qdfn_problem {
+    int64_t N;              /* FaultCount */
+    int64_t Nload;          /* LoadingFaultCount (the last Nload patches) */
+    int32_t n_inst;         /* instances sharing the operator (1..4) */
+    int32_t evolution_dr;   /* EvolutionDR: 1 aging law, otherwise slip law */
+    const double* a;        /* length n_inst*N each */
+    const double* b;
+    const double* Dc;
+    const double* theta_i;
+    const double* V_i;
+    const double* f_i;      /* FrictionI */
+    const double* sigma0;   /* InitialNormalStress */
+    const double* V_const;  /* LoadingRate */
+    const double* mass;     /* Mass */
+    double G;               /* ShearModulus */
+    double rho;             /* RockDensity */
+    double sigma_min;       /* MinimumNormalStress */
+    double switch_v;        /* SwitchV */
+    double dt_cut;          /* DtCut */
+    double rupture_dt;      /* RuptureDt */
+    double max_dt;          /* MaximumDt */
+    double alpha_evo;       /* Alpha_Evo */
+    int32_t interp_at_told; /* 0: external stress at TOld+Dt (main); 1: at TOld (main_H) */
+    int32_t reserved;
+    int64_t record_step;    /* RecordStep (0 = no history) */
+    int64_t max_records;    /* capacity of the history buffers, in records */
+} qdfn_problem;
+
+/* Creates a context (device allocations) and initialises the state the way
+ * main()/main_H() do before their step loop. */
+int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* p);
+int qdfn_ctx_destroy(qdfn_ctx* ctx);
+
+/* Dense operator.  Ks/Kn are N x N in `layout` with leading dimension ld.
+ * Forms ElasticLoadingShearMatrix = K_ij/K_ii (zero diagonal) and K_Self =
+ * |K_ii| as main() does (Functions_RSFDFN3DMain_D.jl:53-67) and stores both
+ * matrices in `precision` (QDFN_FP64, QDFN_FP32, QDFN_BF16X2). */
+int qdfn_set_dense(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_t ld, int layout,
+                   int precision);
+
+/* H-matrix operator (Functions_Hmatrix.jl).  nb blocks; range is nb x 4
+ * {src_begin, src_end, recv_begin, recv_end}, 0-based inclusive (the
+ * reference's ElementRange_SR minus one).  For block b and each of the shear (s)
+ * and normal (n) matrices: rank < 0 -> dense block D (recv x src, row-major);
+ * rank >= 0 -> low-rank U (recv x rank) * Vt (rank x src), both row-major.
+ * Diagonal blocks must be dense; K_Self = -K_ii and the diagonal of the shear
+ * blocks is zeroed (StiffnessTransitionToLoading, Functions_Hmatrix.jl:459-477). */
+int qdfn_set_hmatrix(qdfn_ctx* ctx, int64_t nb, const int64_t* range, const int64_t* rank_s,
+                     const double* const* U_s, const double* const* Vt_s,
+                     const double* const* D_s, const int64_t* rank_n,
+                     const double* const* U_n, const double* const* Vt_n,
+                     const double* const* D_n, int precision);
+
+/* External stress history (Input_ExternalStressChange.jld2): nt samples of
+ * time t[nt] and nt x N row-major normal, shear and pressure changes, shared by
+ * all instances.  Interpolated as InterpolateFromStressChange
+ * (Functions_Solvers.jl:465-540). */
+int qdfn_set_external_stress(qdfn_ctx* ctx, int64_t nt, const double* t, const double* dsn,
+                             const double* dtau, const double* dp);
+
+/* Advances every instance by nsteps time steps.  timeout_s bounds the wall time
+ * of the call (0 = no bound); on expiry the device loop stops at its next
+ * barrier and QDFN_ERR_TIMEOUT is returned.  A failing instance stops the run
+ * and its status is returned. */
+int qdfn_run(qdfn_ctx* ctx, int64_t nsteps, double timeout_s);
+/* As qdfn_run, enqueued on `stream` without waiting; query with qdfn_sync. */
+int qdfn_run_async(qdfn_ctx* ctx, int64_t nsteps, double timeout_s, void* stream);
+int qdfn_sync(qdfn_ctx* ctx);
+
+/* Number of device kernels one qdfn_run launches (for launch accounting). */
+int qdfn_kernels_per_run(const qdfn_ctx* ctx);
+
+/* State of one instance (host copies).  Any pointer may be NULL. */
+int qdfn_get_state(const qdfn_ctx* ctx, int inst, double* V, double* D, double* theta,
+                   double* friction, double* accel, double* sigma_old, double* T, double* dt,
+                   int64_t* step);
+int qdfn_set_state(qdfn_ctx* ctx, int inst, const double* V, const double* D,
+                   const double* theta, const double* friction, const double* accel,
+                   const double* sigma_old, double T, double dt, int64_t step);
+
+/* History of one instance: records 0..*nrec-1 (History_Time, History_Dt and the
+ * record x N arrays History_V/_Disp/_Theta/_NormalStress).  Any pointer may be
+ * NULL; nrec receives the number of records written so far. */
+int qdfn_get_history(const qdfn_ctx* ctx, int inst, double* T, double* Dt, double* V, double* D,
+                     double* theta, double* sigma, int64_t* nrec);
+
+/* Applies the stored operator once: tld = ElasticLoadingShearMatrix * (0 - D)
+ * and knd = StiffnessMatrixNormal * D for every instance (D, tld, knd are
+ * n_inst x N host arrays).  Exposed for operator-level tests. */
+int qdfn_apply_operator(qdfn_ctx* ctx, const double* D, double* tld, double* knd);
+
+/* K_Self of the stored operator (length N). */
+int qdfn_get_kself(const qdfn_ctx* ctx, double* kself);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QDFN_H */

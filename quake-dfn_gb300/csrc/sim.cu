@@ -1,0 +1,1055 @@
+// Persistent earthquake-cycle kernel and the simulation-context C ABI.
+//
+// One cooperative launch advances every instance of a context by `nsteps` time
+// steps.  Per step (scripts/Functions_RSFDFN3DMain_D.jl:146-322):
+//   P1  solver switch (VOld > SwitchV) and the time-step control reductions
+//       (max V and min |V/Accel| over the unstable patches, :163-187)
+//   --  grid barrier; every CTA reduces the per-CTA partials itself, so all CTAs
+//       hold identical step scalars without another round trip
+//   P2  elastic operator: one pass over the shear (K_ij/K_ii) and normal
+//       matrices computes both products for all instances at once
+//   --  grid barrier
+//   P3  per-patch secant solves (SolveOneTimeStep, Functions_Solvers.jl:334),
+//       then the retry decision (:240-253) -- repeated until every instance
+//       accepts its step
+//   P4  history record, T += Dt, Accel, state rotation (:265-319)
+// Grid barriers are a counter/generation pair with a bounded wait on
+// %globaltimer: a wait that outlives the deadline sets QDFN_ERR_TIMEOUT and the
+// kernel returns.  The launch is cooperative, so all CTAs are co-resident.
+#include <cooperative_groups.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "qdfn_internal.h"
+#include "sim_device.cuh"
+
+namespace qdfn {
+namespace {
+
+constexpr int kSimThreads = 256;
+constexpr int kMaxInst = 4;
+constexpr int kRedSlots = 8;                // doubles per (CTA, instance) partial
+constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
+
+// ---------------------------------------------------------------------------
+// matrix element formats: each thread owns VEC consecutive receiver rows and
+// loads them with one 16-byte access per source column.
+struct FmtF64 {
+    static constexpr int VEC = 2;
+    using X = double;  // staged x type
+    __device__ __forceinline__ static void load(const void* base, int64_t off, double v[2]) {
+        const double2 q = __ldg(reinterpret_cast<const double2*>(reinterpret_cast<const double*>(base) + off));
+        v[0] = q.x; v[1] = q.y;
+    }
+};
+struct FmtF32 {
+    static constexpr int VEC = 4;
+    using X = float;
+    __device__ __forceinline__ static void load(const void* base, int64_t off, float v[4]) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float*>(base) + off));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+};
+struct FmtBF16x2 {  // each 32-bit word: hi bf16 in the upper half, lo bf16 in the lower half
+    static constexpr int VEC = 4;
+    using X = float;
+    __device__ __forceinline__ static void load(const void* base, int64_t off, float v[4]) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(base) + off));
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            v[k] = __uint_as_float(w[k] & 0xFFFF0000u) + __uint_as_float(w[k] << 16);
+    }
+};
+
+struct SimParams {
+    int64_t N, Nload, ld;
+    int R;
+    int evolution_dr, interp_at_told, hmat;
+    double eta, sigma_min, switch_v, dt_cut, rupture_dt, max_dt, alpha_evo;
+    int64_t record_step, max_records;
+    // per [R][N] constants
+    const double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega;
+    const double* kself;             // [N]
+    const unsigned char* unstable;   // [R][N]
+    const int* has_unstable;         // [R]
+    // external stress
+    int64_t n_ext;
+    const double *ext_t, *ext_n, *ext_s, *ext_p;
+    // dense operator, source-major: entry (recv i, src j) at j*ld + i
+    const void* E;
+    const void* Kn;
+    int nchunk;                      // column chunks of the matvec
+    int64_t chunk_len;
+    // state [R][N]
+    double *V, *D, *theta, *fric, *accel, *sig_old;
+    double *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
+    int *instab, *flag, *sw;
+    double *part_s, *part_n;         // [nchunk][R][N]
+    // scalars [R]
+    double *T, *dt;
+    int64_t *step, *nrec;
+    int* status;                     // [R]
+    // history [R][max_records][N] and [R][max_records]
+    double *hT, *hDt, *hV, *hD, *hth, *hs;
+    // barrier + reductions
+    unsigned *bar_count, *bar_gen;
+    double* red;                     // [2][nblocks][R][kRedSlots]
+    int* gerr;
+    uint64_t budget_ns;             // wall-time budget of this launch
+};
+
+// bounded grid barrier; returns false on timeout (all CTAs then return)
+__device__ bool grid_barrier(const SimParams& p, uint64_t deadline_ns) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = p.bar_gen;
+        const unsigned my_gen = *gen;
+        __threadfence();
+        const unsigned prev = atomicAdd(p.bar_count, 1u);
+        int ok = 1;
+        if (prev == gridDim.x - 1) {
+            atomicExch(p.bar_count, 0u);
+            __threadfence();
+            atomicAdd((unsigned*)p.bar_gen, 1u);
+        } else {
+            while (*gen == my_gen) {
+                if (globaltimer_ns() > deadline_ns + 2000000000ull) { ok = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (!ok) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// block-wide reduction of R*K doubles with op (0 = max, 1 = min, 2 = sum)
+template <int K>
+__device__ void block_reduce(double (&v)[kMaxInst][K], const int (&ops)[K], int R) {
+    __shared__ double s_buf[kSimThreads / 32][kMaxInst][K];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double x = v[r][k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double y = __shfl_xor_sync(0xffffffffu, x, o);
+                x = ops[k] == 0 ? fmax(x, y) : ops[k] == 1 ? fmin(x, y) : x + y;
+            }
+            if (lane == 0) s_buf[wid][r][k] = x;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                double x = s_buf[0][r][k];
+                for (int w = 1; w < kSimThreads / 32; ++w) {
+                    const double y = s_buf[w][r][k];
+                    x = ops[k] == 0 ? fmax(x, y) : ops[k] == 1 ? fmin(x, y) : x + y;
+                }
+                v[r][k] = x;
+            }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// P2: dense elastic operator.  Tile = (row block of kSimThreads*VEC receivers,
+// column chunk).  x = D staged in shared memory; both matrices read once for all
+// R instances.  FP32 products are summed in FP32 over 32 columns, then folded
+// into FP64 accumulators (FP64 formats accumulate in FP64 directly).
+template <class M, int R>
+__device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
+    using X = typename M::X;
+    constexpr int VEC = M::VEC;
+    constexpr int64_t rows_per_blk = (int64_t)kSimThreads * VEC;
+    const int64_t N = p.N;
+    const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
+    const int64_t ntiles = nrb * p.nchunk;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t rb = tile % nrb, c = tile / nrb;
+        const int64_t j0 = c * p.chunk_len;
+        const int64_t j1 = min(N, j0 + p.chunk_len);
+        const int64_t L = j1 - j0;
+        __syncthreads();
+        for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kSimThreads) {
+            const int r = (int)(q / L);
+            const int64_t j = q % L;
+            xs[r * p.chunk_len + j] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
+        }
+        __syncthreads();
+        const int64_t i0 = rb * rows_per_blk + (int64_t)threadIdx.x * VEC;
+        if (i0 < N) {
+            double as[R][VEC], an[R][VEC];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) { as[r][v] = 0.0; an[r][v] = 0.0; }
+            const int64_t base = j0 * p.ld + i0;
+            if constexpr (sizeof(X) == 8) {
+                int64_t j = 0;
+                for (; j + 4 <= L; j += 4) {
+                    double e[4][VEC], k[4][VEC];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        M::load(p.E, base + (j + u) * p.ld, e[u]);
+                        M::load(p.Kn, base + (j + u) * p.ld, k[u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const double x = xs[r * p.chunk_len + j + u];
+#pragma unroll
+                            for (int v = 0; v < VEC; ++v) {
+                                as[r][v] = fma(e[u][v], x, as[r][v]);
+                                an[r][v] = fma(k[u][v], x, an[r][v]);
+                            }
+                        }
+                }
+                for (; j < L; ++j) {
+                    double e[VEC], k[VEC];
+                    M::load(p.E, base + j * p.ld, e);
+                    M::load(p.Kn, base + j * p.ld, k);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const double x = xs[r * p.chunk_len + j];
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) {
+                            as[r][v] = fma(e[v], x, as[r][v]);
+                            an[r][v] = fma(k[v], x, an[r][v]);
+                        }
+                    }
+                }
+            } else {
+                int64_t j = 0;
+                while (j < L) {
+                    const int64_t jend = min(L, j + 32);
+                    float fs[R][VEC], fn[R][VEC];
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) { fs[r][v] = 0.f; fn[r][v] = 0.f; }
+                    for (; j + 4 <= jend; j += 4) {
+                        float e[4][VEC], k[4][VEC];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            M::load(p.E, base + (j + u) * p.ld, e[u]);
+                            M::load(p.Kn, base + (j + u) * p.ld, k[u]);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+#pragma unroll
+                            for (int r = 0; r < R; ++r) {
+                                const float x = xs[r * p.chunk_len + j + u];
+#pragma unroll
+                                for (int v = 0; v < VEC; ++v) {
+                                    fs[r][v] = fmaf(e[u][v], x, fs[r][v]);
+                                    fn[r][v] = fmaf(k[u][v], x, fn[r][v]);
+                                }
+                            }
+                    }
+                    for (; j < jend; ++j) {
+                        float e[VEC], k[VEC];
+                        M::load(p.E, base + j * p.ld, e);
+                        M::load(p.Kn, base + j * p.ld, k);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const float x = xs[r * p.chunk_len + j];
+#pragma unroll
+                            for (int v = 0; v < VEC; ++v) {
+                                fs[r][v] = fmaf(e[v], x, fs[r][v]);
+                                fn[r][v] = fmaf(k[v], x, fn[r][v]);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) {
+                            as[r][v] += (double)fs[r][v];
+                            an[r][v] += (double)fn[r][v];
+                        }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) {
+                    const int64_t i = i0 + v;
+                    if (i < N) {
+                        const int64_t o = ((int64_t)c * R + r) * N + i;
+                        p.part_s[o] = as[r][v];
+                        p.part_n[o] = an[r][v];
+                    }
+                }
+        }
+    }
+}
+
+template <class M, int R>
+__global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nsteps) {
+    extern __shared__ unsigned char smem_raw[];
+    using X = typename M::X;
+    X* xs = reinterpret_cast<X*>(smem_raw);
+    __shared__ double s_T[kMaxInst], s_dt[kMaxInst];
+    __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
+    __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop;
+    __shared__ int s_iter;
+    // each CTA measures the budget from its own start; the P1 reduction makes
+    // the stop decision common to all CTAs
+    const uint64_t deadline = globaltimer_ns() + p.budget_ns;
+    const int64_t N = p.N, Ns = p.N - p.Nload;
+    const int64_t nthreads = (int64_t)gridDim.x * kSimThreads;
+    const int64_t gtid = (int64_t)blockIdx.x * kSimThreads + threadIdx.x;
+    int phase = 0;  // parity selector of the reduction buffer
+    if (threadIdx.x < R) {
+        s_T[threadIdx.x] = p.T[threadIdx.x];
+        s_dt[threadIdx.x] = p.dt[threadIdx.x];
+        s_step[threadIdx.x] = p.step[threadIdx.x];
+        s_nrec[threadIdx.x] = p.nrec[threadIdx.x];
+        s_fail[threadIdx.x] = p.status[threadIdx.x];
+    }
+    if (threadIdx.x == 0) s_stop = 0;
+    __syncthreads();
+    auto red_slot = [&](int ph, int64_t blk, int r) -> double* {
+        return p.red + (((int64_t)(ph & 1) * gridDim.x + blk) * R + r) * kRedSlots;
+    };
+
+    for (int64_t it = 0; it < nsteps; ++it) {
+        // ---------------------------------------------------------- P1
+        {
+            double v[kMaxInst][4];
+            int errloc = 0;
+            for (int r = 0; r < R; ++r) { v[r][0] = -INFINITY; v[r][1] = 0; v[r][2] = INFINITY; v[r][3] = 0; }
+            for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+                const int r = (int)(q / N);
+                const int64_t i = q - (int64_t)r * N;
+                const double Vo = p.V[q];
+                p.sw[q] = Vo > p.switch_v ? 1 : 0;
+                const bool ctl = p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns);
+                if (ctl) {
+                    if (isnan(Vo)) v[r][1] = 1;
+                    else v[r][0] = fmax(v[r][0], Vo);
+                    const double qa = fabs(Vo / p.accel[q]);
+                    if (!isnan(qa) && qa != 0) { v[r][3] = 1; v[r][2] = fmin(v[r][2], qa); }
+                }
+            }
+            (void)errloc;
+            const int ops[4] = {0, 0, 1, 0};
+            block_reduce<4>(v, ops, R);
+            if (threadIdx.x == 0) {
+                for (int r = 0; r < R; ++r) {
+                    double* s = red_slot(phase, blockIdx.x, r);
+                    s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
+                    s[4] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
+                }
+            }
+            if (!grid_barrier(p, deadline)) return;
+            if (threadIdx.x < R) {
+                const int r = threadIdx.x;
+                double vmax = -INFINITY, vnan = 0, dtmin = INFINITY, any = 0, late = 0;
+                for (int b = 0; b < (int)gridDim.x; ++b) {
+                    const double* s = red_slot(phase, b, r);
+                    vmax = fmax(vmax, __ldcg(s)); vnan = fmax(vnan, __ldcg(s + 1));
+                    dtmin = fmin(dtmin, __ldcg(s + 2)); any = fmax(any, __ldcg(s + 3));
+                    late = fmax(late, __ldcg(s + 4));
+                }
+                if (late != 0) s_stop = 1;   // benign race: every writer stores 1
+                if (vnan != 0) vmax = NAN;
+                if (any == 0 && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
+                dtmin = dtmin / p.dt_cut;
+                double DtRef;
+                if (vmax > p.switch_v) DtRef = p.rupture_dt;
+                else if (dtmin > p.max_dt) DtRef = p.max_dt;
+                else DtRef = dtmin;
+                double Dt = s_dt[r];
+                if (DtRef <= p.rupture_dt) Dt = DtRef;
+                else if (Dt < DtRef / 1.2) Dt = Dt * 1.2;
+                else Dt = DtRef;
+                s_dt[r] = Dt;
+                s_done[r] = 0;
+            }
+            phase++;
+            __syncthreads();
+            int stop = s_stop;
+            for (int r = 0; r < R; ++r) stop |= (s_fail[r] != 0);
+            if (stop) break;
+        }
+        // ---------------------------------------------------------- P2
+        dense_matvec<M, R>(p, xs);
+        if (!grid_barrier(p, deadline)) return;
+        // ---------------------------------------------------------- P3
+        if (threadIdx.x == 0) s_iter = 0;
+        __syncthreads();
+        for (;;) {
+            double v[kMaxInst][4];
+            for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
+            const int first = (s_iter == 0);
+            for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+                const int r = (int)(q / N);
+                if (s_done[r]) continue;
+                const int64_t i = q - (int64_t)r * N;
+                if (first) {
+                    double ss = 0, sn = 0;
+                    for (int c = 0; c < p.nchunk; ++c) {
+                        ss += __ldcg(p.part_s + ((int64_t)c * R + r) * N + i);
+                        sn += __ldcg(p.part_n + ((int64_t)c * R + r) * N + i);
+                    }
+                    p.tld[q] = -ss;   // ELSM * (0 - DispOld)
+                    p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
+                }
+                const double Dt = s_dt[r];
+                double dsn = 0, dss = 0, dsp = 0;
+                if (p.n_ext > 0) {
+                    const double tq = p.interp_at_told ? s_T[r] : s_T[r] + Dt;
+                    sim::interp_ext(p.n_ext, p.ext_t, p.ext_n, p.ext_s, p.ext_p, N, i, tq, dsn, dss, dsp);
+                }
+                double sig = p.knd[q] + p.sigma0[q] + dsn;
+                if (sig < p.sigma_min) sig = p.sigma_min;
+                if (i < Ns) {
+                    sim::PatchIn pin;
+                    pin.DispOld = p.D[q]; pin.FrictionOld = p.fric[q]; pin.ThetaOld = p.theta[q];
+                    pin.VOld = p.V[q]; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
+                    pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
+                    pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
+                    pin.dtau = dss; pin.sigma_old = p.sig_old[q]; pin.tau0 = p.tau0[q];
+                    int err = 0;
+                    const sim::PatchOut o = p.sw[q] == 1
+                        ? sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err)
+                        : sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
+                    p.Vn[q] = o.V; p.fn[q] = o.Friction; p.Dn[q] = o.Disp; p.thn[q] = o.Theta;
+                    p.sn[q] = sig; p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
+                    if (err) v[r][3] = fmin(v[r][3], (double)err);
+                    v[r][0] = fmin(v[r][0], (double)o.Flag);
+                    v[r][1] = fmin(v[r][1], o.Dt);
+                    if (o.Instab == 4) v[r][2] = 1;
+                    if (o.Flag == 0) {   // Main_D :242-249, applied by the patch's owner
+                        if (o.Instab == 3) p.sw[q] = 1;
+                        else if (o.Instab == 4) p.sw[q] = 0;
+                    }
+                } else {                 // loading faults (Solvers :370-377)
+                    const double Vc = p.Vconst[q];
+                    p.Vn[q] = Vc; p.fn[q] = p.fric[q]; p.Dn[q] = p.D[q] + Vc * Dt;
+                    p.thn[q] = p.theta[q]; p.sn[q] = 1e10; p.dtall[q] = Dt;
+                    p.instab[q] = 0; p.flag[q] = 1;
+                    v[r][1] = fmin(v[r][1], Dt);
+                }
+            }
+            const int ops[4] = {1, 1, 0, 1};
+            block_reduce<4>(v, ops, R);
+            if (threadIdx.x == 0)
+                for (int r = 0; r < R; ++r) {
+                    double* s = red_slot(phase, blockIdx.x, r);
+                    s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
+                }
+            if (!grid_barrier(p, deadline)) return;
+            if (threadIdx.x < R) {
+                const int r = threadIdx.x;
+                if (!s_done[r]) {
+                    double mflag = 1, mdt = INFINITY, any4 = 0, err = 0;
+                    for (int b = 0; b < (int)gridDim.x; ++b) {
+                        const double* s = red_slot(phase, b, r);
+                        mflag = fmin(mflag, __ldcg(s)); mdt = fmin(mdt, __ldcg(s + 1));
+                        any4 = fmax(any4, __ldcg(s + 2)); err = fmin(err, __ldcg(s + 3));
+                    }
+                    if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
+                    else if (mflag == 0) {
+                        s_dt[r] = any4 != 0 ? 1e-3 : mdt;
+                    } else {
+                        s_dt[r] = mdt;   // Main_D :262 Dt = minimum(Dt_All)
+                        s_done[r] = 1;
+                    }
+                }
+            }
+            phase++;
+            if (threadIdx.x == 0) s_iter++;
+            __syncthreads();
+            int all = 1;
+            for (int r = 0; r < R; ++r) all &= s_done[r];
+            if (all) break;
+            if (s_iter > kRetryCap) {
+                if (threadIdx.x < R && !s_done[threadIdx.x]) s_fail[threadIdx.x] = QDFN_ERR_RETRIES;
+                __syncthreads();
+                break;
+            }
+        }
+        {
+            int anyfail = 0;
+            for (int r = 0; r < R; ++r) anyfail |= (s_fail[r] != 0);
+            if (anyfail) break;
+        }
+        // ---------------------------------------------------------- P4
+        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+            const int r = (int)(q / N);
+            const int64_t i = q - (int64_t)r * N;
+            const double Dt = s_dt[r];
+            const int64_t gstep = s_step[r] + 1;
+            if (p.record_step > 0 && gstep % p.record_step == 0 && s_nrec[r] < p.max_records) {
+                const int64_t o = ((int64_t)r * p.max_records + s_nrec[r]) * N + i;
+                p.hV[o] = p.Vn[q]; p.hD[o] = p.Dn[q]; p.hth[o] = p.thn[q]; p.hs[o] = p.sn[q];
+                if (i == 0) {
+                    p.hT[(int64_t)r * p.max_records + s_nrec[r]] = s_T[r];
+                    p.hDt[(int64_t)r * p.max_records + s_nrec[r]] = Dt;
+                }
+            }
+            p.accel[q] = (p.Vn[q] - p.V[q]) / Dt;
+            p.D[q] = p.Dn[q];
+            p.theta[q] = p.thn[q];
+            p.V[q] = p.Vn[q];
+            p.fric[q] = p.fn[q];
+            p.sig_old[q] = p.sn[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < R) {
+            const int r = threadIdx.x;
+            const int64_t gstep = s_step[r] + 1;
+            if (p.record_step > 0 && gstep % p.record_step == 0 && s_nrec[r] < p.max_records)
+                s_nrec[r]++;
+            s_T[r] = s_T[r] + s_dt[r];
+            s_step[r] = gstep;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x < R) {
+        const int r = threadIdx.x;
+        p.T[r] = s_T[r];
+        p.dt[r] = s_dt[r];
+        p.step[r] = s_step[r];
+        p.nrec[r] = s_nrec[r];
+        p.status[r] = s_fail[r];
+        if (s_stop && s_fail[r] == 0) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+    }
+}
+
+// Operator-only kernel (qdfn_apply_operator): one pass of P2 + chunk reduction.
+template <class M, int R>
+__global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    using X = typename M::X;
+    dense_matvec<M, R>(p, reinterpret_cast<X*>(smem_raw));
+}
+
+__global__ void k_chunk_reduce(SimParams p) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (int64_t)p.R * p.N) return;
+    const int r = (int)(q / p.N);
+    const int64_t i = q - (int64_t)r * p.N;
+    double ss = 0, sn = 0;
+    for (int c = 0; c < p.nchunk; ++c) {
+        ss += p.part_s[((int64_t)c * p.R + r) * p.N + i];
+        sn += p.part_n[((int64_t)c * p.R + r) * p.N + i];
+    }
+    p.tld[q] = -ss;
+    p.knd[q] = sn;
+}
+
+// ---------------------------------------------------------------------------
+// conversion kernels: source-major storage of ELSM and Kn in the chosen format
+__global__ void k_convert(const double* __restrict__ Ks, const double* __restrict__ Knm,
+                          int64_t N, int64_t ld_in, int layout, int64_t ld, int prec,
+                          void* E, void* Kn, double* kself) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // receiver
+    const int64_t j = blockIdx.y;                                        // source (loops)
+    for (int64_t jj = j; jj < N; jj += gridDim.y) {
+        if (i >= ld) continue;
+        double e = 0.0, k = 0.0;
+        if (i < N) {
+            const int64_t in = layout == QDFN_LAYOUT_COL ? jj * ld_in + i : i * ld_in + jj;
+            const int64_t dd = layout == QDFN_LAYOUT_COL ? i * ld_in + i : i * ld_in + i;
+            const double kii = Ks[dd];
+            e = (i == jj) ? 0.0 : Ks[in] / kii;   // Main_D :58-62
+            k = Knm[in];
+            if (jj == 0) kself[i] = fabs(kii);
+        }
+        const int64_t o = jj * ld + i;
+        if (prec == QDFN_FP64) {
+            reinterpret_cast<double*>(E)[o] = e;
+            reinterpret_cast<double*>(Kn)[o] = k;
+        } else if (prec == QDFN_FP32) {
+            reinterpret_cast<float*>(E)[o] = (float)e;
+            reinterpret_cast<float*>(Kn)[o] = (float)k;
+        } else {
+            auto split = [](double x) -> uint32_t {
+                const __nv_bfloat16 hi = __double2bfloat16(x);
+                const double rem = x - (double)__bfloat162float(hi);
+                const __nv_bfloat16 lo = __double2bfloat16(rem);
+                return ((uint32_t)__bfloat16_as_ushort(hi) << 16) | (uint32_t)__bfloat16_as_ushort(lo);
+            };
+            reinterpret_cast<uint32_t*>(E)[o] = split(e);
+            reinterpret_cast<uint32_t*>(Kn)[o] = split(k);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace qdfn
+
+// ===========================================================================
+// Context
+using namespace qdfn;
+
+struct qdfn_ctx {
+    int64_t N = 0, Nload = 0, ld = 0;
+    int R = 1;
+    int prec = -1;
+    int hmat = 0;
+    qdfn_problem prob{};
+    double eta = 0;
+    // device buffers
+    std::vector<void*> allocs;
+    double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega, *kself;
+    unsigned char* unstable;
+    int* has_unstable;
+    double *V, *D, *theta, *fric, *accel, *sig_old, *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
+    int *instab, *flag, *sw;
+    double *part_s = nullptr, *part_n = nullptr;
+    double *T, *dt;
+    int64_t *step, *nrec;
+    int* status;
+    double *hT, *hDt, *hV, *hD, *hth, *hs;
+    unsigned *bar_count, *bar_gen;
+    double* red = nullptr;
+    int* gerr;
+    void* E = nullptr;
+    void* Kn = nullptr;
+    int64_t n_ext = 0;
+    double *ext_t = nullptr, *ext_n = nullptr, *ext_s = nullptr, *ext_p = nullptr;
+    int nblocks = 0, nchunk = 1;
+    int64_t chunk_len = 0;
+    size_t smem = 0;
+    cudaStream_t pending = nullptr;
+    bool running = false;
+
+    template <class T>
+    int dalloc(T** p, size_t n) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, n * sizeof(T) + 16) != cudaSuccess)
+            return fail(QDFN_ERR_NOMEM, "cudaMalloc failed");
+        cudaMemset(q, 0, n * sizeof(T) + 16);
+        allocs.push_back(q);
+        *p = reinterpret_cast<T*>(q);
+        return QDFN_OK;
+    }
+    void release(void* q) {
+        if (!q) return;
+        auto it = std::find(allocs.begin(), allocs.end(), q);
+        if (it != allocs.end()) { cudaFree(q); allocs.erase(it); }
+    }
+    ~qdfn_ctx() {
+        for (void* q : allocs) cudaFree(q);
+    }
+};
+
+namespace {
+
+// kernel instance count is rounded up to 1, 2, 4; extra instances replicate
+// instance 0 and are ignored
+int kernel_R(int R) { return R <= 1 ? 1 : R <= 2 ? 2 : 4; }
+
+int h2d(void* dst, const void* src, size_t bytes) {
+    QDFN_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return QDFN_OK;
+}
+
+SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
+    SimParams p{};
+    p.N = c->N; p.Nload = c->Nload; p.ld = c->ld; p.R = kernel_R(c->R);
+    p.evolution_dr = c->prob.evolution_dr; p.interp_at_told = c->prob.interp_at_told; p.hmat = c->hmat;
+    p.eta = c->eta; p.sigma_min = c->prob.sigma_min; p.switch_v = c->prob.switch_v;
+    p.dt_cut = c->prob.dt_cut; p.rupture_dt = c->prob.rupture_dt; p.max_dt = c->prob.max_dt;
+    p.alpha_evo = c->prob.alpha_evo;
+    p.record_step = c->prob.record_step; p.max_records = c->prob.max_records;
+    p.a = c->a; p.b = c->b; p.Dc = c->Dc; p.F0 = c->F0; p.tau0 = c->tau0; p.sigma0 = c->sigma0;
+    p.Vconst = c->Vconst; p.mass = c->mass; p.omega = c->omega; p.kself = c->kself;
+    p.unstable = c->unstable; p.has_unstable = c->has_unstable;
+    p.n_ext = c->n_ext; p.ext_t = c->ext_t; p.ext_n = c->ext_n; p.ext_s = c->ext_s; p.ext_p = c->ext_p;
+    p.E = c->E; p.Kn = c->Kn; p.nchunk = c->nchunk; p.chunk_len = c->chunk_len;
+    p.V = c->V; p.D = c->D; p.theta = c->theta; p.fric = c->fric; p.accel = c->accel; p.sig_old = c->sig_old;
+    p.Vn = c->Vn; p.Dn = c->Dn; p.thn = c->thn; p.fn = c->fn; p.sn = c->sn; p.dtall = c->dtall;
+    p.tld = c->tld; p.knd = c->knd; p.instab = c->instab; p.flag = c->flag; p.sw = c->sw;
+    p.part_s = c->part_s; p.part_n = c->part_n;
+    p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
+    p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
+    p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
+    p.budget_ns = budget_ns;
+    return p;
+}
+
+using SimKernel = void (*)(SimParams, int64_t);
+using ApplyKernel = void (*)(SimParams);
+
+template <class M>
+SimKernel pick_sim(int R) {
+    switch (R) {
+        case 1: return k_sim<M, 1>;
+        case 2: return k_sim<M, 2>;
+        default: return k_sim<M, 4>;
+    }
+}
+SimKernel sim_kernel(int prec, int R) {
+    if (prec == QDFN_FP64) return pick_sim<FmtF64>(R);
+    if (prec == QDFN_FP32) return pick_sim<FmtF32>(R);
+    return pick_sim<FmtBF16x2>(R);
+}
+template <class M>
+ApplyKernel pick_apply(int R) {
+    switch (R) {
+        case 1: return k_apply<M, 1>;
+        case 2: return k_apply<M, 2>;
+        default: return k_apply<M, 4>;
+    }
+}
+ApplyKernel apply_kernel(int prec, int R) {
+    if (prec == QDFN_FP64) return pick_apply<FmtF64>(R);
+    if (prec == QDFN_FP32) return pick_apply<FmtF32>(R);
+    return pick_apply<FmtBF16x2>(R);
+}
+
+
+int configure_launch(qdfn_ctx* c) {
+    const int Rk = kernel_R(c->R);
+    const int vec = c->prec == QDFN_FP64 ? 2 : 4;
+    const size_t xsz = c->prec == QDFN_FP64 ? 8 : 4;
+    const int sms = num_sms();
+    if (sms <= 0) return fail(QDFN_ERR_CUDA, "no CUDA device");
+    SimKernel k = sim_kernel(c->prec, c->R);
+    // chunk length: at most 2048 columns staged in shared memory per instance
+    const int64_t rows_per_blk = (int64_t)kSimThreads * vec;
+    const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
+    // aim for >= 2 tiles per SM
+    int64_t want_chunks = std::max<int64_t>(1, (2LL * sms + nrb - 1) / nrb);
+    int64_t clen = (c->N + want_chunks - 1) / want_chunks;
+    clen = std::min<int64_t>(std::max<int64_t>(clen, 64), 2048);
+    c->chunk_len = clen;
+    c->nchunk = (int)((c->N + clen - 1) / clen);
+    c->smem = (size_t)Rk * clen * xsz;
+    QDFN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    int occ = 0;
+    QDFN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kSimThreads, c->smem));
+    if (occ < 1) return fail(QDFN_ERR_CUDA, "simulation kernel cannot be resident");
+    const int64_t work_items = (int64_t)Rk * c->N;
+    int64_t nb = std::min<int64_t>((int64_t)sms * occ, std::max<int64_t>(1, nrb * c->nchunk));
+    nb = std::max<int64_t>(1, std::min<int64_t>(nb, (work_items + 31) / 32));
+    if (c->nblocks > 0) nb = std::min<int64_t>(nb, c->nblocks);
+    c->nblocks = (int)nb;
+    ApplyKernel ka = apply_kernel(c->prec, c->R);
+    QDFN_CUDA(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    // buffers sized by the launch shape
+    c->release(c->part_s);
+    c->release(c->part_n);
+    c->release(c->red);
+    int rc;
+    if ((rc = c->dalloc(&c->part_s, (size_t)c->nchunk * Rk * c->N))) return rc;
+    if ((rc = c->dalloc(&c->part_n, (size_t)c->nchunk * Rk * c->N))) return rc;
+    if ((rc = c->dalloc(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots))) return rc;
+    return QDFN_OK;
+}
+
+}  // namespace
+
+extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
+    if (!out || !pr) return fail(QDFN_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const int64_t N = pr->N;
+    if (N < 1) return fail(QDFN_ERR_INVALID, "N must be >= 1");
+    if (pr->Nload < 0 || pr->Nload > N) return fail(QDFN_ERR_INVALID, "Nload out of range");
+    if (pr->n_inst < 1 || pr->n_inst > kMaxInst) return fail(QDFN_ERR_INVALID, "n_inst must be 1..4");
+    if (!pr->a || !pr->b || !pr->Dc || !pr->theta_i || !pr->V_i || !pr->f_i || !pr->sigma0 ||
+        !pr->V_const || !pr->mass)
+        return fail(QDFN_ERR_INVALID, "null per-patch array");
+    if (pr->record_step < 0 || pr->max_records < 0) return fail(QDFN_ERR_INVALID, "negative record sizes");
+    if (!(pr->G > 0) || !(pr->rho > 0)) return fail(QDFN_ERR_INVALID, "G and rho must be positive");
+    auto* c = new qdfn_ctx();
+    c->N = N; c->Nload = pr->Nload; c->R = pr->n_inst; c->prob = *pr;
+    c->eta = pr->G / 2 / std::sqrt(pr->G / pr->rho);
+    const int Rk = kernel_R(c->R);
+    const size_t RN = (size_t)Rk * N;
+    int rc = 0;
+#define A(ptr, n) if (!rc) rc = c->dalloc(&c->ptr, n)
+    A(a, RN); A(b, RN); A(Dc, RN); A(F0, RN); A(tau0, RN); A(sigma0, RN); A(Vconst, RN);
+    A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
+    A(V, RN); A(D, RN); A(theta, RN); A(fric, RN); A(accel, RN); A(sig_old, RN);
+    A(Vn, RN); A(Dn, RN); A(thn, RN); A(fn, RN); A(sn, RN); A(dtall, RN); A(tld, RN); A(knd, RN);
+    A(instab, RN); A(flag, RN); A(sw, RN);
+    A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
+    const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
+    A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
+    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1);
+#undef A
+    if (rc) { delete c; return rc; }
+    // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
+    std::vector<double> ha(RN), hb(RN), hDc(RN), hF0(RN), htau0(RN), hs0(RN), hVc(RN), hm(RN),
+        hth(RN), hV(RN), hf(RN), hzero(RN, 0.0);
+    std::vector<unsigned char> hun(RN);
+    std::vector<int> hhas(Rk, 0);
+    for (int r = 0; r < Rk; ++r) {
+        const int src = r < c->R ? r : 0;
+        for (int64_t i = 0; i < N; ++i) {
+            const size_t q = (size_t)r * N + i, s = (size_t)src * N + i;
+            ha[q] = pr->a[s]; hb[q] = pr->b[s]; hDc[q] = pr->Dc[s];
+            hth[q] = pr->theta_i[s]; hV[q] = pr->V_i[s]; hf[q] = pr->f_i[s];
+            hs0[q] = pr->sigma0[s]; hVc[q] = pr->V_const[s]; hm[q] = pr->mass[s];
+            if (pr->V_i[s] / sim::kV0 < 0 || pr->theta_i[s] * sim::kV0 / pr->Dc[s] < 0) {
+                delete c;
+                return fail(QDFN_ERR_DOMAIN, "log of a negative number in Friction0");
+            }
+            hF0[q] = pr->f_i[s] - pr->a[s] * std::log(pr->V_i[s] / sim::kV0) -
+                     pr->b[s] * std::log(pr->theta_i[s] * sim::kV0 / pr->Dc[s]);
+            htau0[q] = pr->sigma0[s] * pr->f_i[s];
+            hun[q] = (pr->a[s] - pr->b[s] < 0) ? 1 : 0;
+            if (hun[q]) hhas[r] = 1;
+        }
+    }
+    std::vector<double> ones(Rk, 1.0), zeros(Rk, 0.0);
+    std::vector<int64_t> z64(Rk, 0);
+    std::vector<int> z32(Rk, 0);
+    if ((rc = h2d(c->a, ha.data(), RN * 8)) || (rc = h2d(c->b, hb.data(), RN * 8)) ||
+        (rc = h2d(c->Dc, hDc.data(), RN * 8)) || (rc = h2d(c->F0, hF0.data(), RN * 8)) ||
+        (rc = h2d(c->tau0, htau0.data(), RN * 8)) || (rc = h2d(c->sigma0, hs0.data(), RN * 8)) ||
+        (rc = h2d(c->Vconst, hVc.data(), RN * 8)) || (rc = h2d(c->mass, hm.data(), RN * 8)) ||
+        (rc = h2d(c->unstable, hun.data(), RN)) || (rc = h2d(c->has_unstable, hhas.data(), Rk * 4)) ||
+        (rc = h2d(c->V, hV.data(), RN * 8)) || (rc = h2d(c->theta, hth.data(), RN * 8)) ||
+        (rc = h2d(c->fric, hf.data(), RN * 8)) || (rc = h2d(c->sig_old, hs0.data(), RN * 8)) ||
+        (rc = h2d(c->D, hzero.data(), RN * 8)) || (rc = h2d(c->accel, hzero.data(), RN * 8)) ||
+        (rc = h2d(c->T, zeros.data(), Rk * 8)) || (rc = h2d(c->dt, ones.data(), Rk * 8)) ||
+        (rc = h2d(c->step, z64.data(), Rk * 8)) || (rc = h2d(c->nrec, z64.data(), Rk * 8)) ||
+        (rc = h2d(c->status, z32.data(), Rk * 4))) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_ctx_destroy(qdfn_ctx* ctx) {
+    if (!ctx) return QDFN_OK;
+    if (ctx->running) cudaStreamSynchronize(ctx->pending);
+    delete ctx;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_set_dense(qdfn_ctx* c, const double* Ks, const double* Kn, int64_t ld_in,
+                              int layout, int precision) {
+    if (!c || !Ks || !Kn) return fail(QDFN_ERR_INVALID, "null argument");
+    if (precision != QDFN_FP64 && precision != QDFN_FP32 && precision != QDFN_BF16X2)
+        return fail(QDFN_ERR_INVALID, "unknown precision");
+    if (layout != QDFN_LAYOUT_ROW && layout != QDFN_LAYOUT_COL)
+        return fail(QDFN_ERR_INVALID, "unknown layout");
+    const int64_t N = c->N;
+    if (ld_in < N) return fail(QDFN_ERR_INVALID, "ld < N");
+    // K_ii must be nonzero for K_ij/K_ii
+    for (int64_t i = 0; i < N; ++i)
+        if (Ks[i * ld_in + i] == 0.0) return fail(QDFN_ERR_INVALID, "zero self stiffness K_ii");
+    c->release(c->E);
+    c->release(c->Kn);
+    c->E = c->Kn = nullptr;
+    c->prec = precision;
+    c->hmat = 0;
+    c->ld = (N + 31) / 32 * 32;
+    const size_t esz = precision == QDFN_FP64 ? 8 : 4;
+    const size_t mbytes = (size_t)N * c->ld * esz;
+    unsigned char *dE = nullptr, *dK = nullptr;
+    int rc = c->dalloc(&dE, mbytes);
+    if (!rc) rc = c->dalloc(&dK, mbytes);
+    if (rc) return rc;
+    c->E = dE;
+    c->Kn = dK;
+    // stage the FP64 input once on the device and convert there
+    double *tS = nullptr, *tN = nullptr;
+    const size_t inbytes = (size_t)N * ld_in * sizeof(double);
+    if (cudaMalloc(&tS, inbytes) != cudaSuccess) return fail(QDFN_ERR_NOMEM, "staging buffer");
+    if (cudaMalloc(&tN, inbytes) != cudaSuccess) { cudaFree(tS); return fail(QDFN_ERR_NOMEM, "staging buffer"); }
+    cudaError_t e1 = cudaMemcpy(tS, Ks, inbytes, cudaMemcpyHostToDevice);
+    cudaError_t e2 = cudaMemcpy(tN, Kn, inbytes, cudaMemcpyHostToDevice);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        cudaFree(tS); cudaFree(tN);
+        return cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaMemcpy (set_dense)");
+    }
+    dim3 grid((unsigned)((c->ld + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
+    k_convert<<<grid, 256>>>(tS, tN, N, ld_in, layout, c->ld, precision, c->E, c->Kn, c->kself);
+    cudaError_t ek = cudaGetLastError();
+    if (ek == cudaSuccess) ek = cudaDeviceSynchronize();
+    cudaFree(tS);
+    cudaFree(tN);
+    if (ek != cudaSuccess) return cuda_fail(ek, "k_convert");
+    // Omega = sqrt(K_Self / M) (Main_D :56)
+    std::vector<double> ks(N), m((size_t)kernel_R(c->R) * N), om(m.size());
+    QDFN_CUDA(cudaMemcpy(ks.data(), c->kself, N * 8, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(m.data(), c->mass, m.size() * 8, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < m.size(); ++q) {
+        const double x = ks[q % N] / m[q];
+        if (x < 0) return fail(QDFN_ERR_DOMAIN, "sqrt of a negative number in Omega");
+        om[q] = std::sqrt(x);
+    }
+    if ((rc = h2d(c->omega, om.data(), om.size() * 8))) return rc;
+    return configure_launch(c);
+}
+
+extern "C" int qdfn_set_external_stress(qdfn_ctx* c, int64_t nt, const double* t,
+                                        const double* dsn, const double* dtau, const double* dp) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (nt < 0) return fail(QDFN_ERR_INVALID, "nt < 0");
+    c->release(c->ext_t); c->release(c->ext_n); c->release(c->ext_s); c->release(c->ext_p);
+    c->ext_t = c->ext_n = c->ext_s = c->ext_p = nullptr;
+    c->n_ext = 0;
+    if (nt == 0) return QDFN_OK;
+    if (!t || !dsn || !dtau || !dp) return fail(QDFN_ERR_INVALID, "null external-stress array");
+    int rc;
+    const size_t n = (size_t)nt * c->N;
+    if ((rc = c->dalloc(&c->ext_t, nt)) || (rc = c->dalloc(&c->ext_n, n)) ||
+        (rc = c->dalloc(&c->ext_s, n)) || (rc = c->dalloc(&c->ext_p, n)))
+        return rc;
+    if ((rc = h2d(c->ext_t, t, nt * 8)) || (rc = h2d(c->ext_n, dsn, n * 8)) ||
+        (rc = h2d(c->ext_s, dtau, n * 8)) || (rc = h2d(c->ext_p, dp, n * 8)))
+        return rc;
+    c->n_ext = nt;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_run_async(qdfn_ctx* c, int64_t nsteps, double timeout_s, void* stream) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (c->prec < 0) return fail(QDFN_ERR_STATE, "no operator set (qdfn_set_dense first)");
+    if (nsteps < 0) return fail(QDFN_ERR_INVALID, "nsteps < 0");
+    if (nsteps == 0) return QDFN_OK;
+    const double budget = timeout_s > 0 ? timeout_s : 1e6;
+    const uint64_t budget_ns = (uint64_t)(budget * 1e9);
+    cudaStream_t st = (cudaStream_t)stream;
+    QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, sizeof(int), st));
+    QDFN_CUDA(cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), st));
+    SimParams p = make_params(c, budget_ns);
+    SimKernel k = sim_kernel(c->prec, c->R);
+    void* args[] = {&p, &nsteps};
+    QDFN_CUDA(cudaLaunchCooperativeKernel((const void*)k, dim3(c->nblocks), dim3(kSimThreads), args,
+                                          c->smem, st));
+    c->pending = st;
+    c->running = true;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_sync(qdfn_ctx* c) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (!c->running) return QDFN_OK;
+    c->running = false;
+    QDFN_CUDA(cudaStreamSynchronize(c->pending));
+    int gerr = 0;
+    QDFN_CUDA(cudaMemcpy(&gerr, c->gerr, sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> st(kernel_R(c->R));
+    QDFN_CUDA(cudaMemcpy(st.data(), c->status, st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int r = 0; r < c->R; ++r)
+        if (st[r] != 0) return fail(st[r], "instance " + std::to_string(r) + " stopped");
+    if (gerr != 0) return fail(gerr, "device loop stopped early");
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_run(qdfn_ctx* c, int64_t nsteps, double timeout_s) {
+    int rc = qdfn_run_async(c, nsteps, timeout_s, nullptr);
+    if (rc) return rc;
+    return qdfn_sync(c);
+}
+
+extern "C" int qdfn_kernels_per_run(const qdfn_ctx* c) { return c ? 1 : 0; }
+
+extern "C" int qdfn_get_state(const qdfn_ctx* c, int inst, double* V, double* D, double* theta,
+                              double* friction, double* accel, double* sigma_old, double* T,
+                              double* dt, int64_t* step) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (inst < 0 || inst >= c->R) return fail(QDFN_ERR_INVALID, "instance out of range");
+    const size_t off = (size_t)inst * c->N, n = (size_t)c->N * 8;
+    if (V) QDFN_CUDA(cudaMemcpy(V, c->V + off, n, cudaMemcpyDeviceToHost));
+    if (D) QDFN_CUDA(cudaMemcpy(D, c->D + off, n, cudaMemcpyDeviceToHost));
+    if (theta) QDFN_CUDA(cudaMemcpy(theta, c->theta + off, n, cudaMemcpyDeviceToHost));
+    if (friction) QDFN_CUDA(cudaMemcpy(friction, c->fric + off, n, cudaMemcpyDeviceToHost));
+    if (accel) QDFN_CUDA(cudaMemcpy(accel, c->accel + off, n, cudaMemcpyDeviceToHost));
+    if (sigma_old) QDFN_CUDA(cudaMemcpy(sigma_old, c->sig_old + off, n, cudaMemcpyDeviceToHost));
+    if (T) QDFN_CUDA(cudaMemcpy(T, c->T + inst, 8, cudaMemcpyDeviceToHost));
+    if (dt) QDFN_CUDA(cudaMemcpy(dt, c->dt + inst, 8, cudaMemcpyDeviceToHost));
+    if (step) QDFN_CUDA(cudaMemcpy(step, c->step + inst, 8, cudaMemcpyDeviceToHost));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_set_state(qdfn_ctx* c, int inst, const double* V, const double* D,
+                              const double* theta, const double* friction, const double* accel,
+                              const double* sigma_old, double T, double dt, int64_t step) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (inst < 0 || inst >= c->R) return fail(QDFN_ERR_INVALID, "instance out of range");
+    const size_t off = (size_t)inst * c->N, n = (size_t)c->N * 8;
+    if (V) QDFN_CUDA(cudaMemcpy(c->V + off, V, n, cudaMemcpyHostToDevice));
+    if (D) QDFN_CUDA(cudaMemcpy(c->D + off, D, n, cudaMemcpyHostToDevice));
+    if (theta) QDFN_CUDA(cudaMemcpy(c->theta + off, theta, n, cudaMemcpyHostToDevice));
+    if (friction) QDFN_CUDA(cudaMemcpy(c->fric + off, friction, n, cudaMemcpyHostToDevice));
+    if (accel) QDFN_CUDA(cudaMemcpy(c->accel + off, accel, n, cudaMemcpyHostToDevice));
+    if (sigma_old) QDFN_CUDA(cudaMemcpy(c->sig_old + off, sigma_old, n, cudaMemcpyHostToDevice));
+    QDFN_CUDA(cudaMemcpy(c->T + inst, &T, 8, cudaMemcpyHostToDevice));
+    QDFN_CUDA(cudaMemcpy(c->dt + inst, &dt, 8, cudaMemcpyHostToDevice));
+    QDFN_CUDA(cudaMemcpy(c->step + inst, &step, 8, cudaMemcpyHostToDevice));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_get_history(const qdfn_ctx* c, int inst, double* T, double* Dt, double* V,
+                                double* D, double* theta, double* sigma, int64_t* nrec) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (inst < 0 || inst >= c->R) return fail(QDFN_ERR_INVALID, "instance out of range");
+    int64_t n = 0;
+    QDFN_CUDA(cudaMemcpy(&n, c->nrec + inst, 8, cudaMemcpyDeviceToHost));
+    if (nrec) *nrec = n;
+    if (n == 0) return QDFN_OK;
+    const size_t off1 = (size_t)inst * c->prob.max_records;
+    const size_t offN = off1 * c->N;
+    const size_t bytesN = (size_t)n * c->N * 8;
+    if (T) QDFN_CUDA(cudaMemcpy(T, c->hT + off1, n * 8, cudaMemcpyDeviceToHost));
+    if (Dt) QDFN_CUDA(cudaMemcpy(Dt, c->hDt + off1, n * 8, cudaMemcpyDeviceToHost));
+    if (V) QDFN_CUDA(cudaMemcpy(V, c->hV + offN, bytesN, cudaMemcpyDeviceToHost));
+    if (D) QDFN_CUDA(cudaMemcpy(D, c->hD + offN, bytesN, cudaMemcpyDeviceToHost));
+    if (theta) QDFN_CUDA(cudaMemcpy(theta, c->hth + offN, bytesN, cudaMemcpyDeviceToHost));
+    if (sigma) QDFN_CUDA(cudaMemcpy(sigma, c->hs + offN, bytesN, cudaMemcpyDeviceToHost));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, double* knd) {
+    if (!c || !D || !tld || !knd) return fail(QDFN_ERR_INVALID, "null argument");
+    if (c->prec < 0) return fail(QDFN_ERR_STATE, "no operator set");
+    const size_t n = (size_t)c->R * c->N * 8;
+    std::vector<double> saved(n / 8);
+    QDFN_CUDA(cudaMemcpy(saved.data(), c->D, n, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(c->D, D, n, cudaMemcpyHostToDevice));
+    SimParams p = make_params(c, 0);
+    apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
+    QDFN_CUDA(cudaGetLastError());
+    const int64_t tot = (int64_t)c->R * c->N;
+    k_chunk_reduce<<<(unsigned)((tot + 255) / 256), 256>>>(p);
+    QDFN_CUDA(cudaGetLastError());
+    QDFN_CUDA(cudaDeviceSynchronize());
+    QDFN_CUDA(cudaMemcpy(tld, c->tld, n, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(knd, c->knd, n, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(c->D, saved.data(), n, cudaMemcpyHostToDevice));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_get_kself(const qdfn_ctx* c, double* kself) {
+    if (!c || !kself) return fail(QDFN_ERR_INVALID, "null argument");
+    if (c->prec < 0) return fail(QDFN_ERR_STATE, "no operator set");
+    QDFN_CUDA(cudaMemcpy(kself, c->kself, c->N * 8, cudaMemcpyDeviceToHost));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, const int64_t* rank_s,
+                                const double* const* U_s, const double* const* Vt_s,
+                                const double* const* D_s, const int64_t* rank_n,
+                                const double* const* U_n, const double* const* Vt_n,
+                                const double* const* D_n, int precision) {
+    (void)c; (void)nb; (void)range; (void)rank_s; (void)U_s; (void)Vt_s; (void)D_s;
+    (void)rank_n; (void)U_n; (void)Vt_n; (void)D_n; (void)precision;
+    return fail(QDFN_ERR_STATE, "H-matrix operator not available in this build");
+}

@@ -1,0 +1,114 @@
+"""ctypes binding of libqdfn.so (the C ABI declared in include/qdfn.h).
+
+There is no CPU fallback: every compute entry point runs the CUDA library, and
+loading fails loudly when the library has not been built.
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int64)
+_pdp = C.POINTER(_dp)
+
+QDFN_OK = 0
+ERRORS = {
+    -1: "QDFN_ERR_INVALID", -2: "QDFN_ERR_CUDA", -3: "QDFN_ERR_NOMEM", -4: "QDFN_ERR_STATE",
+    -10: "QDFN_ERR_DOMAIN", -11: "QDFN_ERR_EMPTY", -12: "QDFN_ERR_RETRIES", -13: "QDFN_ERR_NO_CONVERGE",
+    -14: "QDFN_ERR_TIMEOUT", -15: "QDFN_ERR_HALF_SPACE",
+}
+LAYOUT_ROW, LAYOUT_COL = 0, 1
+FP64, FP32, BF16X2 = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x2": BF16X2}
+
+# every symbol include/qdfn.h declares
+EXPORTS = [
+    "qdfn_version", "qdfn_status_string", "qdfn_last_error",
+    "qdfn_assemble_rect", "qdfn_assemble_rect_dev", "qdfn_assemble_tri", "qdfn_assemble_tri_dev",
+    "qdfn_ctx_create", "qdfn_ctx_destroy", "qdfn_set_dense", "qdfn_set_hmatrix",
+    "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
+    "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
+]
+
+
+class QdfnError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "QDFN_ERR"), code, msg))
+        self.code = code
+
+
+class Problem(C.Structure):
+    """Mirror of struct qdfn_problem."""
+    _fields_ = [("N", C.c_int64), ("Nload", C.c_int64), ("n_inst", C.c_int32), ("evolution_dr", C.c_int32)] + \
+               [(n, _dp) for n in ("a", "b", "Dc", "theta_i", "V_i", "f_i", "sigma0", "V_const", "mass")] + \
+               [(n, C.c_double) for n in ("G", "rho", "sigma_min", "switch_v", "dt_cut", "rupture_dt", "max_dt",
+                                          "alpha_evo")] + \
+               [("interp_at_told", C.c_int32), ("reserved", C.c_int32), ("record_step", C.c_int64),
+                ("max_records", C.c_int64)]
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB_PATH
+
+
+def load():
+    """Load libqdfn.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError("libqdfn.so not found at %s; build it with "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    L = C.CDLL(path)
+    L.qdfn_version.restype = C.c_char_p
+    L.qdfn_status_string.restype = C.c_char_p
+    L.qdfn_status_string.argtypes = [C.c_int]
+    L.qdfn_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    L.qdfn_assemble_rect.argtypes = [C.c_int64, _dp, C.c_int64, _dp, C.c_double, C.c_double, _dp, _dp, C.c_int]
+    L.qdfn_assemble_rect_dev.argtypes = [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_double, C.c_double,
+                                         C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+    L.qdfn_assemble_tri.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int64, _dp, _dp, _dp, C.c_double,
+                                    C.c_double, _dp, _dp, C.c_int]
+    L.qdfn_assemble_tri_dev.argtypes = [C.c_int64] + [C.c_void_p] * 4 + [C.c_int64] + [C.c_void_p] * 3 + \
+                                       [C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_int64, C.c_int,
+                                        C.c_void_p]
+    L.qdfn_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Problem)]
+    L.qdfn_ctx_destroy.argtypes = [C.c_void_p]
+    L.qdfn_set_dense.argtypes = [C.c_void_p, _dp, _dp, C.c_int64, C.c_int, C.c_int]
+    L.qdfn_set_hmatrix.argtypes = [C.c_void_p, C.c_int64, _ip, _ip, _pdp, _pdp, _pdp, _ip, _pdp, _pdp, _pdp, C.c_int]
+    L.qdfn_set_external_stress.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp]
+    L.qdfn_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]
+    L.qdfn_run_async.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
+    L.qdfn_sync.argtypes = [C.c_void_p]
+    L.qdfn_kernels_per_run.argtypes = [C.c_void_p]
+    L.qdfn_get_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 8 + [_ip]
+    L.qdfn_set_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [C.c_double, C.c_double, C.c_int64]
+    L.qdfn_get_history.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [_ip]
+    L.qdfn_apply_operator.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    L.qdfn_get_kself.argtypes = [C.c_void_p, _dp]
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    load().qdfn_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc):
+    if rc != QDFN_OK:
+        raise QdfnError(rc, last_error())
+    return rc
+
+
+def dp(a):
+    """double* of a C-contiguous float64 numpy array (or NULL for None)."""
+    if a is None:
+        return _dp()
+    return a.ctypes.data_as(_dp)
