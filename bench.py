@@ -1,0 +1,446 @@
+"""Benchmark: ensemble simulated-years per wall-clock hour of the earthquake-cycle
+step loop on GB300.
+
+Workload (default): the 30-fault random network (seed 2, 100 m patches,
+12,813 rectangular patches; shapes of the reference's fault-network config),
+four friction draws on that geometry advanced together as one ensemble, elastic
+operator stored in FP32 (mixed precision) with FP64 state, friction inversion
+and time control.  Synthetic, seeded input: the reference ships no benchmark
+data.  A bench "step" is one adaptive time step of every ensemble member.
+
+  value     device-resident: one persistent launch advances the ensemble K steps
+            (inputs already in HBM), CUDA events on the launch stream
+  e2e       the same K steps through the C ABI with host buffers: every step
+            uploads the ensemble state from pinned host memory
+            (qdfn_set_state), runs one step (qdfn_run) and reads the state back
+            (qdfn_get_state)
+  fp64_gpu  the same window with the operator in FP64, one instance per launch
+            (the plain FP64 GPU path), and the slip error of the mixed run
+            against it
+  cpu_baseline  the FP64 CPU oracle (restatement of the reference algorithm)
+            on a bounded sample of the same window, all host threads
+
+--impl reference times that CPU oracle on the whole window (the reference is
+Julia, which is not available; the oracle restates its algorithm in C++).
+Under torchrun each rank runs an independent replica (the path does not shard:
+"replicas only"); value sums the ranks' simulated years over the slowest rank.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "quake-dfn_gb300"))
+
+YEAR = 365.25 * 24 * 3600.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16x2", "fp64"])
+    ap.add_argument("--inst", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--faults", type=int, default=30)
+    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    ap.add_argument("--ref-instances", type=int, default=1,
+                    help="ensemble members the CPU reference arm times (a bounded sample)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(args):
+    from qdfn import synth
+    sysd = synth.fault_network(seed=args.seed, n_faults=args.faults)
+    draws = synth.friction_draws(sysd, args.inst, seed=1)
+    return sysd, draws
+
+
+def problem(sysd, draws, kdiag, n_inst):
+    from qdfn import synth
+    return synth.problem_dict(sysd, kdiag, n_inst=n_inst, draws=draws)
+
+
+def ext_ramp(sysd):
+    from qdfn import synth
+    return synth.external_ramp(sysd["N"], sysd["stressing_rate"], 1e12)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=float(np.median(sm)), sm_max_mhz=float(np.max(smax)), reasons=sorted(reasons),
+                       samples=len(sm))
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per simulation step of the kernel from a committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_sim_network_fp32_r4.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def total_sim_time(sim, n):
+    return np.array([sim.state(r)["T"] for r in range(n)])
+
+
+def run_ours(args):
+    import torch
+    from qdfn import _lib, assemble, simulate
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sysd, draws = workload(args)
+    N, R = sysd["N"], args.inst
+
+    # stiffness on the device (FP64 Okada), column-major like Julia's K[recv, src]
+    rec = torch.tensor(sysd["records"], dtype=torch.float64, device=dev)
+    Ks = torch.empty((N, N), dtype=torch.float64, device=dev)
+    Kn = torch.empty((N, N), dtype=torch.float64, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    assemble.assemble_rect_dev(rec, rec, sysd["G"], sysd["nu"], Ks, Kn, stream=stream.cuda_stream, layout="col")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    asm_ms = e0.elapsed_time(e1)
+    kdiag = torch.diagonal(Ks).cpu().numpy()
+    prob = problem(sysd, draws, kdiag, R)
+    ext = ext_ramp(sysd)
+
+    sim = simulate.Simulation(prob, n_inst=R)
+    sim.set_dense_device(Ks, Kn, args.precision, layout="col", stream=stream.cuda_stream)
+    sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+    sim64 = None
+    if not args.no_fp64:
+        p1 = problem(sysd, {k: v[:N] for k, v in draws.items()}, kdiag, 1)
+        sim64 = simulate.Simulation(p1, n_inst=1)
+        sim64.set_dense_device(Ks, Kn, "fp64", layout="col", stream=stream.cuda_stream)
+        sim64.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+    Ks_host = Kn_host = None
+    if rank == 0 and not args.no_cpu:
+        Ks_host = Ks.cpu().numpy()  # (src, recv) memory = K[recv, src] column-major -> transpose view
+        Kn_host = Kn.cpu().numpy()
+    del Ks, Kn
+    torch.cuda.empty_cache()
+
+    # warm-up (untimed): the first W steps of the trajectory
+    sim.run(args.warmup)
+    if sim64 is not None:
+        sim64.run(args.warmup)
+    start_states = [sim.state(r) for r in range(R)]
+    T0 = np.array([s["T"] for s in start_states])
+
+    # ---- timed: one persistent launch over K steps
+    clocks = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.run_async(args.steps, stream=stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sim.sync()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    T1 = total_sim_time(sim, R)
+    sim_years = float(np.sum(T1 - T0)) / YEAR
+    end_state0 = sim.state(0)
+    if ws > 1:
+        t = torch.tensor([sim_years], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t)
+        sim_years_all = float(t.item())
+    else:
+        sim_years_all = sim_years
+    value = sim_years_all / (ms / 1e3 / 3600.0)
+
+    # ---- roofline of the persistent kernel (dominant, and the only kernel of the run)
+    esz = {"fp32": 4, "bf16x2": 4, "fp64": 8}[args.precision]
+    ld = (N + 31) // 32 * 32
+    mat_bytes = 2 * N * ld * esz
+    vec_bytes = R * N * 8 * 14       # state read/write + matvec partials, per step
+    alg_bytes = args.steps * (mat_bytes + vec_bytes)
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    prof = profiled_traffic()
+    traffic = None
+    if prof and prof.get("N") == N and prof.get("precision") == args.precision and prof.get("inst") == R:
+        traffic = float(prof["dram_bytes_per_step"]) * args.steps
+
+    # ---- FP64 GPU path on the same window (draw 0 alone)
+    fp64 = None
+    if sim64 is not None:
+        s0 = sim64.state(0)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        sim64.run_async(args.steps, stream=stream.cuda_stream)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        sim64.sync()
+        ms64 = f0.elapsed_time(f1)
+        s1 = sim64.state(0)
+        yrs64 = (s1["T"] - s0["T"]) / YEAR
+        slip_err = float(np.max(np.abs(end_state0["D"] - s1["D"])) / max(np.max(np.abs(s1["D"])), 1e-300))
+        fp64 = {"value": yrs64 / (ms64 / 1e3 / 3600.0), "ms_per_step": ms64 / args.steps, "instances": 1,
+                "slip_rel_err_vs_fp64": slip_err, "mixed_over_fp64": (value / max(ws, 1)) / (yrs64 / (ms64 / 3.6e6))}
+
+    # ---- e2e through the C ABI with host buffers, same window
+    e2e = None
+    if not args.no_e2e:
+        L = _lib.load()
+        for r in range(R):
+            sim.set_state(r, start_states[r])
+        pin = {k: [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(R)]
+               for k in ("V", "D", "theta", "friction", "accel", "sigma_old")}
+        for r in range(R):
+            for k in pin:
+                pin[k][r].copy_(torch.from_numpy(np.ascontiguousarray(start_states[r][k])))
+        Ts = [C.c_double(start_states[r]["T"]) for r in range(R)]
+        dts = [C.c_double(start_states[r]["dt"]) for r in range(R)]
+        steps = [C.c_int64(start_states[r]["step"]) for r in range(R)]
+        P = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+        names = ("V", "D", "theta", "friction", "accel", "sigma_old")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for r in range(R):
+                _lib.check(L.qdfn_set_state(sim._h, r, *(P(pin[k][r]) for k in names), Ts[r].value, dts[r].value,
+                                            steps[r].value))
+            _lib.check(L.qdfn_run(sim._h, 1, 0.0))
+            for r in range(R):
+                _lib.check(L.qdfn_get_state(sim._h, r, *(P(pin[k][r]) for k in names), C.byref(Ts[r]),
+                                            C.byref(dts[r]), C.byref(steps[r])))
+        t_e2e = time.perf_counter() - t0
+        yrs = sum(Ts[r].value - start_states[r]["T"] for r in range(R)) / YEAR
+        per_inst = 6 * N * 8 + 3 * 8
+        e2e = {"value": (yrs * max(ws, 1)) / (t_e2e / 3600.0), "unit": "sim-years/hour",
+               "h2d_bytes_per_step": R * per_inst, "d2h_bytes_per_step": R * per_inst}
+
+    # ---- CPU baseline: oracle on a bounded sample of the window
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(args, sysd, draws, kdiag, Ks_host, Kn_host, start_states, ext)
+
+    if rank == 0:
+        line = {
+            "metric": "ensemble sim-years/hour, mixed-prec vs FP64 on GPU at <=1e-6 rel slip error",
+            "value": value, "unit": "sim-years/hour", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32-operator/fp64-state" if args.precision != "fp64" else "fp64",
+            "data": "synthetic (seeded fault network; the reference ships no benchmark data)",
+            "config": {"workload": "fault network, %d faults seed %d, %d rectangular patches, %d friction draws "
+                                   "(ensemble), operator %s, external stressing 0.01 MPa/yr"
+                                   % (args.faults, args.seed, N, R, args.precision),
+                       "patches": N, "instances": R, "precision": args.precision, "parallelism": "replicas",
+                       "l2": "operator %.2f GB per step > 129 MB L2 (no flush needed)" % (mat_bytes / 1e9),
+                       "sim_years_in_window": sim_years_all},
+            "gpu_launches": sim.kernels_per_run(),
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "note": "k_sim persistent kernel, algorithmic bytes = K x (2 N ld x %d B operator + "
+                                 "state vectors); peak %s" % (esz, peak_kind)},
+            "cpu_baseline": cpu,
+            "fp64_gpu": fp64,
+            "assembly": {"pairs": N * N, "ms": asm_ms, "pairs_per_s": N * N / (asm_ms / 1e3)},
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(args, sysd, draws, kdiag, Ks_cm, Kn_cm, start_states, ext):
+    """Oracle (FP64, OpenMP on all host cores) from the window's start state for
+    a bounded number of steps; sim-years/hour of the ensemble on that sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    N, R = sysd["N"], args.inst
+    Ks = Ks_cm.T  # device buffer was (src, recv): K[recv, src] = buf[src, recv]
+    Kn = Kn_cm.T
+    nth = os.cpu_count()
+    sims = []
+    shared = None
+    for r in range(R):
+        p = problem(sysd, {k: v[r * N:(r + 1) * N] for k, v in draws.items()}, kdiag, 1)
+        p.update(ext_t=ext["t"], ext_n=ext["normal"], ext_s=ext["shear"], ext_p=ext["pressure"])
+        s = oracle.Simulation(p, ("dense", Ks, Kn) if shared is None else ("shared", shared), nthreads=nth)
+        shared = s if shared is None else shared
+        st = start_states[r]
+        for k in ("V", "D", "theta", "friction", "accel", "sigma_old"):
+            s.state[k][:] = st[k]
+        s.set_scalars(st["T"], st["dt"], st["step"])
+        sims.append(s)
+    T0 = np.array([s.T for s in sims])
+    t0 = time.perf_counter()
+    for s in sims:
+        s.run(1)
+    per_step = time.perf_counter() - t0
+    k = int(max(1, min(args.steps - 1, args.cpu_sample_s / max(per_step, 1e-6))))
+    for s in sims:
+        s.run(k)
+    wall = time.perf_counter() - t0
+    yrs = float(np.sum(np.array([s.T for s in sims]) - T0)) / YEAR
+    return {"value": yrs / (wall / 3600.0), "unit": "sim-years/hour", "cores": nth, "kind": "port",
+            "sample": "first %d steps of the timed window, %d instances, FP64 CPU oracle (C++ restatement of "
+                      "the reference algorithm)" % (k + 1, R), "ms_per_step": wall / (k + 1) * 1e3}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.lib()
+    sysd, draws = workload(args)
+    N, R = sysd["N"], args.inst
+    rec = sysd["records"]
+    cols = dict(cx=rec[:, 0], cy=rec[:, 1], cz=rec[:, 2], ls=rec[:, 3], ld=rec[:, 4], strike=rec[:, 5],
+                dip=rec[:, 6], rake=rec[:, 7])
+    nth = os.cpu_count()
+    Ks, Kn = oracle.assemble_rect(cols, cols, sysd["G"], sysd["nu"], nthreads=nth)
+    kdiag = np.diag(Ks).copy()
+    ext = ext_ramp(sysd)
+    # bounded sample: the first `ref_instances` ensemble members (instances are
+    # independent, so the ensemble rate is their summed simulated time over
+    # their summed wall time)
+    nr = max(1, min(R, args.ref_instances))
+    sims = []
+    shared = None
+    for r in range(nr):
+        p = problem(sysd, {k: v[r * N:(r + 1) * N] for k, v in draws.items()}, kdiag, 1)
+        p.update(ext_t=ext["t"], ext_n=ext["normal"], ext_s=ext["shear"], ext_p=ext["pressure"])
+        s = oracle.Simulation(p, ("dense", Ks, Kn) if shared is None else ("shared", shared), nthreads=nth)
+        shared = s if shared is None else shared
+        sims.append(s)
+    del Ks, Kn
+    for s in sims:
+        s.run(args.warmup)
+    T0 = np.array([s.T for s in sims])
+    t0 = time.perf_counter()
+    for s in sims:
+        s.run(args.steps)
+    wall = time.perf_counter() - t0
+    yrs = float(np.sum(np.array([s.T for s in sims]) - T0)) / YEAR
+    value = yrs / (wall / 3600.0)
+    R = nr
+    line = {"impl": "reference",
+            "metric": "ensemble sim-years/hour, mixed-prec vs FP64 on GPU at <=1e-6 rel slip error",
+            "value": value, "unit": "sim-years/hour", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded fault network)",
+            "config": {"workload": "fault network, %d faults seed %d, %d rectangular patches, %d friction draws "
+                                   "(ensemble), external stressing 0.01 MPa/yr" % (args.faults, args.seed, N, R),
+                       "patches": N, "instances": R, "parallelism": "cpu-threads"},
+            "cpu_baseline": {"value": value, "unit": "sim-years/hour", "cores": nth, "kind": "port",
+                             "sample": "the whole window (%d warm-up + %d timed steps) of %d of the %d ensemble "
+                                       "members, FP64 C++ restatement of the reference algorithm (Julia is not "
+                                       "available)" % (args.warmup, args.steps, R, args.inst)},
+            "e2e": {"value": value, "unit": "sim-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,10 @@ int qdfn_ctx_destroy(qdfn_ctx* ctx);
  * matrices in `precision` (QDFN_FP64, QDFN_FP32, QDFN_BF16X2). */
 int qdfn_set_dense(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_t ld, int layout,
                    int precision);
+/* Device-pointer form of qdfn_set_dense (FP64 Ks/Kn already in device memory,
+ * e.g. straight from qdfn_assemble_rect_dev); the call waits on `stream`. */
+int qdfn_set_dense_dev(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_t ld, int layout,
+                       int precision, void* stream);
 
 /* H-matrix operator (Functions_Hmatrix.jl).  nb blocks; range is nb x 4
  * {src_begin, src_end, recv_begin, recv_end}, 0-based inclusive (the

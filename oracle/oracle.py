@@ -167,11 +167,16 @@ class Simulation:
             pr.n_ext = 0
         self._pr = pr
         kind = operator[0]
+        self._owner = True
         if kind == "dense":
             Ks, Kn = _f64(operator[1]), _f64(operator[2])
             self._op = L.oracle_op_dense(N, _p(Ks), _p(Kn), self.nthreads)
         elif kind == "hmat":
             self._op = self._make_hmat(N, operator[1])
+        elif kind == "shared":  # reuse another Simulation's operator (friction draws)
+            self._op = operator[1]._op
+            self._keep["shared"] = operator[1]
+            self._owner = False
         else:
             raise ValueError(kind)
         self.state = {n: np.zeros(N) for n in ("V", "D", "theta", "friction", "accel", "sigma_old")}
@@ -216,9 +221,14 @@ class Simulation:
 
     def __del__(self):
         try:
-            lib().oracle_op_free(self._op)
+            if self._owner:
+                lib().oracle_op_free(self._op)
         except Exception:
             pass
+
+    def set_scalars(self, T, dt, step):
+        """Time, carried Dt and step count (state arrays are edited in place)."""
+        self._st.T, self._st.dt, self._st.step = float(T), float(dt), int(step)
 
     @property
     def T(self):

@@ -327,11 +327,14 @@ extern "C" void oracle_op_apply(const oracle_operator* op, const double* D, doub
     std::vector<double> x(N);
     for (int64_t j = 0; j < N; ++j) x[j] = 0.0 - D[j];  // Far_Load_Disp_Initial - DispOld
     if (!op->hmat) {
+        // dgemv-like: rows in parallel, each dot product vectorised (the
+        // reference's BLAS dgemv also reorders the sum)
 #pragma omp parallel for schedule(static) num_threads(op->nthreads)
         for (int64_t i = 0; i < N; ++i) {
             const double* e = op->elsm.data() + i * N;
             const double* k = op->kn.data() + i * N;
             double a = 0, c = 0;
+#pragma omp simd reduction(+ : a, c)
             for (int64_t j = 0; j < N; ++j) { a += e[j] * x[j]; c += k[j] * D[j]; }
             tld[i] = a;
             knd[i] = c;

@@ -840,18 +840,12 @@ extern "C" int qdfn_ctx_destroy(qdfn_ctx* ctx) {
     return QDFN_OK;
 }
 
-extern "C" int qdfn_set_dense(qdfn_ctx* c, const double* Ks, const double* Kn, int64_t ld_in,
-                              int layout, int precision) {
-    if (!c || !Ks || !Kn) return fail(QDFN_ERR_INVALID, "null argument");
-    if (precision != QDFN_FP64 && precision != QDFN_FP32 && precision != QDFN_BF16X2)
-        return fail(QDFN_ERR_INVALID, "unknown precision");
-    if (layout != QDFN_LAYOUT_ROW && layout != QDFN_LAYOUT_COL)
-        return fail(QDFN_ERR_INVALID, "unknown layout");
+namespace {
+
+// Converts FP64 Ks/Kn already on the device into the stored operator.
+int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t ld_in, int layout,
+                     int precision, cudaStream_t st) {
     const int64_t N = c->N;
-    if (ld_in < N) return fail(QDFN_ERR_INVALID, "ld < N");
-    // K_ii must be nonzero for K_ij/K_ii
-    for (int64_t i = 0; i < N; ++i)
-        if (Ks[i * ld_in + i] == 0.0) return fail(QDFN_ERR_INVALID, "zero self stiffness K_ii");
     c->release(c->E);
     c->release(c->Kn);
     c->E = c->Kn = nullptr;
@@ -866,7 +860,42 @@ extern "C" int qdfn_set_dense(qdfn_ctx* c, const double* Ks, const double* Kn, i
     if (rc) return rc;
     c->E = dE;
     c->Kn = dK;
-    // stage the FP64 input once on the device and convert there
+    dim3 grid((unsigned)((c->ld + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
+    k_convert<<<grid, 256, 0, st>>>(dKs, dKn, N, ld_in, layout, c->ld, precision, c->E, c->Kn, c->kself);
+    QDFN_CUDA(cudaGetLastError());
+    QDFN_CUDA(cudaStreamSynchronize(st));
+    // Omega = sqrt(K_Self / M) (Main_D :56); K_ii = 0 cannot normalise a row
+    std::vector<double> ks(N), m((size_t)kernel_R(c->R) * N), om(m.size());
+    QDFN_CUDA(cudaMemcpy(ks.data(), c->kself, N * 8, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(m.data(), c->mass, m.size() * 8, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < N; ++i)
+        if (ks[i] == 0.0) return fail(QDFN_ERR_INVALID, "zero self stiffness K_ii");
+    for (size_t q = 0; q < m.size(); ++q) {
+        const double x = ks[q % N] / m[q];
+        if (x < 0) return fail(QDFN_ERR_DOMAIN, "sqrt of a negative number in Omega");
+        om[q] = std::sqrt(x);
+    }
+    if ((rc = h2d(c->omega, om.data(), om.size() * 8))) return rc;
+    return configure_launch(c);
+}
+
+int check_dense_args(qdfn_ctx* c, const void* Ks, const void* Kn, int64_t ld_in, int layout, int precision) {
+    if (!c || !Ks || !Kn) return fail(QDFN_ERR_INVALID, "null argument");
+    if (precision != QDFN_FP64 && precision != QDFN_FP32 && precision != QDFN_BF16X2)
+        return fail(QDFN_ERR_INVALID, "unknown precision");
+    if (layout != QDFN_LAYOUT_ROW && layout != QDFN_LAYOUT_COL)
+        return fail(QDFN_ERR_INVALID, "unknown layout");
+    if (ld_in < c->N) return fail(QDFN_ERR_INVALID, "ld < N");
+    return QDFN_OK;
+}
+
+}  // namespace
+
+extern "C" int qdfn_set_dense(qdfn_ctx* c, const double* Ks, const double* Kn, int64_t ld_in,
+                              int layout, int precision) {
+    int rc = check_dense_args(c, Ks, Kn, ld_in, layout, precision);
+    if (rc) return rc;
+    const int64_t N = c->N;
     double *tS = nullptr, *tN = nullptr;
     const size_t inbytes = (size_t)N * ld_in * sizeof(double);
     if (cudaMalloc(&tS, inbytes) != cudaSuccess) return fail(QDFN_ERR_NOMEM, "staging buffer");
@@ -877,24 +906,17 @@ extern "C" int qdfn_set_dense(qdfn_ctx* c, const double* Ks, const double* Kn, i
         cudaFree(tS); cudaFree(tN);
         return cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaMemcpy (set_dense)");
     }
-    dim3 grid((unsigned)((c->ld + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
-    k_convert<<<grid, 256>>>(tS, tN, N, ld_in, layout, c->ld, precision, c->E, c->Kn, c->kself);
-    cudaError_t ek = cudaGetLastError();
-    if (ek == cudaSuccess) ek = cudaDeviceSynchronize();
+    rc = set_dense_device(c, tS, tN, ld_in, layout, precision, nullptr);
     cudaFree(tS);
     cudaFree(tN);
-    if (ek != cudaSuccess) return cuda_fail(ek, "k_convert");
-    // Omega = sqrt(K_Self / M) (Main_D :56)
-    std::vector<double> ks(N), m((size_t)kernel_R(c->R) * N), om(m.size());
-    QDFN_CUDA(cudaMemcpy(ks.data(), c->kself, N * 8, cudaMemcpyDeviceToHost));
-    QDFN_CUDA(cudaMemcpy(m.data(), c->mass, m.size() * 8, cudaMemcpyDeviceToHost));
-    for (size_t q = 0; q < m.size(); ++q) {
-        const double x = ks[q % N] / m[q];
-        if (x < 0) return fail(QDFN_ERR_DOMAIN, "sqrt of a negative number in Omega");
-        om[q] = std::sqrt(x);
-    }
-    if ((rc = h2d(c->omega, om.data(), om.size() * 8))) return rc;
-    return configure_launch(c);
+    return rc;
+}
+
+extern "C" int qdfn_set_dense_dev(qdfn_ctx* c, const double* Ks, const double* Kn, int64_t ld_in,
+                                  int layout, int precision, void* stream) {
+    int rc = check_dense_args(c, Ks, Kn, ld_in, layout, precision);
+    if (rc) return rc;
+    return set_dense_device(c, Ks, Kn, ld_in, layout, precision, (cudaStream_t)stream);
 }
 
 extern "C" int qdfn_set_external_stress(qdfn_ctx* c, int64_t nt, const double* t,

@@ -26,7 +26,7 @@ PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16x2": BF16X2}
 EXPORTS = [
     "qdfn_version", "qdfn_status_string", "qdfn_last_error",
     "qdfn_assemble_rect", "qdfn_assemble_rect_dev", "qdfn_assemble_tri", "qdfn_assemble_tri_dev",
-    "qdfn_ctx_create", "qdfn_ctx_destroy", "qdfn_set_dense", "qdfn_set_hmatrix",
+    "qdfn_ctx_create", "qdfn_ctx_destroy", "qdfn_set_dense", "qdfn_set_dense_dev", "qdfn_set_hmatrix",
     "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
 ]
@@ -80,6 +80,7 @@ def load():
     L.qdfn_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Problem)]
     L.qdfn_ctx_destroy.argtypes = [C.c_void_p]
     L.qdfn_set_dense.argtypes = [C.c_void_p, _dp, _dp, C.c_int64, C.c_int, C.c_int]
+    L.qdfn_set_dense_dev.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p]
     L.qdfn_set_hmatrix.argtypes = [C.c_void_p, C.c_int64, _ip, _ip, _pdp, _pdp, _pdp, _ip, _pdp, _pdp, _pdp, C.c_int]
     L.qdfn_set_external_stress.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp]
     L.qdfn_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]

@@ -87,6 +87,15 @@ class Simulation:
         Kn_buf = np.ascontiguousarray(Kn_buf)
         _lib.check(self.L.qdfn_set_dense(self._h, _lib.dp(Ks_buf), _lib.dp(Kn_buf), self.N, lay, prec))
 
+    def set_dense_device(self, Ks, Kn, precision="fp64", layout="col", stream=0):
+        """Ks/Kn: float64 CUDA tensors already holding K.  layout="col": shape
+        (N_src, N_recv) contiguous, entry (r, s) at s*N + r (what
+        assemble_rect_dev writes); "row": shape (N_recv, N_src)."""
+        prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        lay = _lib.LAYOUT_COL if layout == "col" else _lib.LAYOUT_ROW
+        _lib.check(self.L.qdfn_set_dense_dev(self._h, Ks.data_ptr(), Kn.data_ptr(), Ks.stride(0), lay, prec,
+                                             C.c_void_p(stream)))
+
     def set_external_stress(self, t, normal, shear, pressure):
         t = _f64(t)
         nt = t.shape[0]

@@ -41,5 +41,7 @@ def oracle_mod():
 @pytest.fixture(scope="session")
 def qdfn_mod():
     import qdfn
+    from qdfn import build
+    build.build()   # no-op when libqdfn.so is newer than its sources
     qdfn.load()
     return qdfn
