@@ -223,12 +223,15 @@ def run_ours(args):
     time.sleep(0.3)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
+    cnt0 = sim.counters()
     sim.run_async(args.steps, stream=stream.cuda_stream)
     ev1.record(stream)
     torch.cuda.synchronize()
     sim.sync()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
+    cnt1 = sim.counters()
+    phases = {k: cnt1[k] - cnt0[k] for k in cnt1}
     if ws > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -335,6 +338,11 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
             "assembly": {"pairs": N * N, "ms": asm_ms, "pairs_per_s": N * N / (asm_ms / 1e3)},
+            "phases_ms_per_step": {"time_control": phases["ns_control"] / 1e6 / args.steps,
+                                   "operator": phases["ns_operator"] / 1e6 / args.steps,
+                                   "friction_solves": phases["ns_solve"] / 1e6 / args.steps,
+                                   "rotation": phases["ns_rotate"] / 1e6 / args.steps,
+                                   "solve_passes_per_step": phases["solve_passes"] / max(phases["steps"], 1)},
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -177,6 +177,10 @@ int qdfn_sync(qdfn_ctx* ctx);
 
 /* Number of device kernels one qdfn_run launches (for launch accounting). */
 int qdfn_kernels_per_run(const qdfn_ctx* ctx);
+/* Cumulative device counters of the context's runs (first n of): ns spent in
+ * [0] time-step control, [1] elastic operator, [2] friction solves and retries,
+ * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps. */
+int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */
 int qdfn_get_state(const qdfn_ctx* ctx, int inst, double* V, double* D, double* theta,

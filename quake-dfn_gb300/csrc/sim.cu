@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "qdfn_internal.h"
+#include "hmat.cuh"
 #include "sim_device.cuh"
 
 namespace qdfn {
@@ -84,6 +85,7 @@ struct SimParams {
     // dense operator, source-major: entry (recv i, src j) at j*ld + i
     const void* E;
     const void* Kn;
+    hmat::Ops h;                     // H-matrix operator (hmat != 0)
     int nchunk;                      // column chunks of the matvec
     int64_t chunk_len;
     // state [R][N]
@@ -102,6 +104,7 @@ struct SimParams {
     double* red;                     // [2][nblocks][R][kRedSlots]
     int* gerr;
     uint64_t budget_ns;             // wall-time budget of this launch
+    unsigned long long* prof;       // [8] cumulative counters (qdfn_get_counters)
 };
 
 // bounded grid barrier; returns false on timeout (all CTAs then return)
@@ -298,11 +301,12 @@ __device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
     }
 }
 
-template <class M, int R>
+template <class M, int R, bool HM>
 __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nsteps) {
     extern __shared__ unsigned char smem_raw[];
     using X = typename M::X;
     X* xs = reinterpret_cast<X*>(smem_raw);
+    double* hacc = reinterpret_cast<double*>(smem_raw + (size_t)R * hmat::kChunk * sizeof(X));
     __shared__ double s_T[kMaxInst], s_dt[kMaxInst];
     __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
     __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop;
@@ -310,6 +314,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     // each CTA measures the budget from its own start; the P1 reduction makes
     // the stop decision common to all CTAs
     const uint64_t deadline = globaltimer_ns() + p.budget_ns;
+    // phase timers of CTA 0 (all CTAs leave each barrier together)
+    uint64_t tp[4] = {0, 0, 0, 0}, tmark = globaltimer_ns();
+    unsigned long long n_iter = 0, n_steps = 0;
+    auto lap = [&](int k) { const uint64_t t = globaltimer_ns(); tp[k] += t - tmark; tmark = t; };
     const int64_t N = p.N, Ns = p.N - p.Nload;
     const int64_t nthreads = (int64_t)gridDim.x * kSimThreads;
     const int64_t gtid = (int64_t)blockIdx.x * kSimThreads + threadIdx.x;
@@ -387,9 +395,17 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             for (int r = 0; r < R; ++r) stop |= (s_fail[r] != 0);
             if (stop) break;
         }
+        lap(0);
         // ---------------------------------------------------------- P2
-        dense_matvec<M, R>(p, xs);
+        if constexpr (HM) {
+            hmat::pass_a<X, R>(p.h, p.D, N, xs, hacc);
+            if (!grid_barrier(p, deadline)) return;
+            hmat::pass_b<X, R>(p.h, p.D, N, xs);
+        } else {
+            dense_matvec<M, R>(p, xs);
+        }
         if (!grid_barrier(p, deadline)) return;
+        lap(1);
         // ---------------------------------------------------------- P3
         if (threadIdx.x == 0) s_iter = 0;
         __syncthreads();
@@ -402,13 +418,20 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 if (s_done[r]) continue;
                 const int64_t i = q - (int64_t)r * N;
                 if (first) {
-                    double ss = 0, sn = 0;
-                    for (int c = 0; c < p.nchunk; ++c) {
-                        ss += __ldcg(p.part_s + ((int64_t)c * R + r) * N + i);
-                        sn += __ldcg(p.part_n + ((int64_t)c * R + r) * N + i);
+                    if constexpr (HM) {
+                        // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
+                        const double ss = hmat::row_sum<R>(p.h, 0, N, i, r);
+                        p.tld[q] = (-ss) / -p.kself[i];
+                        p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
+                    } else {
+                        double ss = 0, sn = 0;
+                        for (int c = 0; c < p.nchunk; ++c) {
+                            ss += __ldcg(p.part_s + ((int64_t)c * R + r) * N + i);
+                            sn += __ldcg(p.part_n + ((int64_t)c * R + r) * N + i);
+                        }
+                        p.tld[q] = -ss;   // ELSM * (0 - DispOld)
+                        p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
                     }
-                    p.tld[q] = -ss;   // ELSM * (0 - DispOld)
-                    p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
                 }
                 const double Dt = s_dt[r];
                 double dsn = 0, dss = 0, dsp = 0;
@@ -474,6 +497,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 }
             }
             phase++;
+            n_iter++;
             if (threadIdx.x == 0) s_iter++;
             __syncthreads();
             int all = 1;
@@ -490,6 +514,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             for (int r = 0; r < R; ++r) anyfail |= (s_fail[r] != 0);
             if (anyfail) break;
         }
+        lap(2);
         // ---------------------------------------------------------- P4
         for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
             const int r = (int)(q / N);
@@ -521,6 +546,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             s_step[r] = gstep;
         }
         __syncthreads();
+        lap(3);
+        n_steps++;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && p.prof) {
+        for (int k = 0; k < 4; ++k) atomicAdd(p.prof + k, (unsigned long long)tp[k]);
+        atomicAdd(p.prof + 4, n_iter);
+        atomicAdd(p.prof + 5, n_steps);
     }
     if (blockIdx.x == 0 && threadIdx.x < R) {
         const int r = threadIdx.x;
@@ -539,6 +571,27 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
     extern __shared__ unsigned char smem_raw[];
     using X = typename M::X;
     dense_matvec<M, R>(p, reinterpret_cast<X*>(smem_raw));
+}
+
+template <class X, int R>
+__global__ void __launch_bounds__(kSimThreads, 1) k_hmat_a(SimParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    hmat::pass_a<X, R>(p.h, p.D, p.N, reinterpret_cast<X*>(smem_raw),
+                       reinterpret_cast<double*>(smem_raw + (size_t)R * hmat::kChunk * sizeof(X)));
+}
+template <class X, int R>
+__global__ void __launch_bounds__(kSimThreads, 1) k_hmat_b(SimParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    hmat::pass_b<X, R>(p.h, p.D, p.N, reinterpret_cast<X*>(smem_raw));
+}
+template <int R>
+__global__ void k_hmat_rows(SimParams p) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (int64_t)R * p.N) return;
+    const int r = (int)(q / p.N);
+    const int64_t i = q - (int64_t)r * p.N;
+    p.tld[q] = (-hmat::row_sum<R>(p.h, 0, p.N, i, r)) / -p.kself[i];
+    p.knd[q] = hmat::row_sum<R>(p.h, 1, p.N, i, r);
 }
 
 __global__ void k_chunk_reduce(SimParams p) {
@@ -622,12 +675,15 @@ struct qdfn_ctx {
     unsigned *bar_count, *bar_gen;
     double* red = nullptr;
     int* gerr;
+    unsigned long long* prof;
     void* E = nullptr;
     void* Kn = nullptr;
     int64_t n_ext = 0;
     double *ext_t = nullptr, *ext_n = nullptr, *ext_s = nullptr, *ext_p = nullptr;
-    int nblocks = 0, nchunk = 1;
+    int nblocks = 0, nblocks_override = 0, nchunk = 1;
     int64_t chunk_len = 0;
+    hmat::Ops hops{};
+    std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
     cudaStream_t pending = nullptr;
     bool running = false;
@@ -683,6 +739,8 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
+    p.prof = c->prof;
+    p.h = c->hops;
     p.budget_ns = budget_ns;
     return p;
 }
@@ -690,18 +748,19 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
 using SimKernel = void (*)(SimParams, int64_t);
 using ApplyKernel = void (*)(SimParams);
 
-template <class M>
+template <class M, bool HM>
 SimKernel pick_sim(int R) {
     switch (R) {
-        case 1: return k_sim<M, 1>;
-        case 2: return k_sim<M, 2>;
-        default: return k_sim<M, 4>;
+        case 1: return k_sim<M, 1, HM>;
+        case 2: return k_sim<M, 2, HM>;
+        default: return k_sim<M, 4, HM>;
     }
 }
-SimKernel sim_kernel(int prec, int R) {
-    if (prec == QDFN_FP64) return pick_sim<FmtF64>(R);
-    if (prec == QDFN_FP32) return pick_sim<FmtF32>(R);
-    return pick_sim<FmtBF16x2>(R);
+SimKernel sim_kernel(int prec, int R, bool hm) {
+    if (hm) return prec == QDFN_FP64 ? pick_sim<FmtF64, true>(R) : pick_sim<FmtF32, true>(R);
+    if (prec == QDFN_FP64) return pick_sim<FmtF64, false>(R);
+    if (prec == QDFN_FP32) return pick_sim<FmtF32, false>(R);
+    return pick_sim<FmtBF16x2, false>(R);
 }
 template <class M>
 ApplyKernel pick_apply(int R) {
@@ -716,7 +775,14 @@ ApplyKernel apply_kernel(int prec, int R) {
     if (prec == QDFN_FP32) return pick_apply<FmtF32>(R);
     return pick_apply<FmtBF16x2>(R);
 }
-
+template <class X>
+void hmat_apply_kernels(int R, ApplyKernel* a, ApplyKernel* b, ApplyKernel* rows) {
+    switch (R) {
+        case 1: *a = k_hmat_a<X, 1>; *b = k_hmat_b<X, 1>; *rows = k_hmat_rows<1>; break;
+        case 2: *a = k_hmat_a<X, 2>; *b = k_hmat_b<X, 2>; *rows = k_hmat_rows<2>; break;
+        default: *a = k_hmat_a<X, 4>; *b = k_hmat_b<X, 4>; *rows = k_hmat_rows<4>; break;
+    }
+}
 
 int configure_launch(qdfn_ctx* c) {
     const int Rk = kernel_R(c->R);
@@ -724,35 +790,54 @@ int configure_launch(qdfn_ctx* c) {
     const size_t xsz = c->prec == QDFN_FP64 ? 8 : 4;
     const int sms = num_sms();
     if (sms <= 0) return fail(QDFN_ERR_CUDA, "no CUDA device");
-    SimKernel k = sim_kernel(c->prec, c->R);
-    // chunk length: at most 2048 columns staged in shared memory per instance
-    const int64_t rows_per_blk = (int64_t)kSimThreads * vec;
-    const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
-    // aim for >= 2 tiles per SM
-    int64_t want_chunks = std::max<int64_t>(1, (2LL * sms + nrb - 1) / nrb);
-    int64_t clen = (c->N + want_chunks - 1) / want_chunks;
-    clen = std::min<int64_t>(std::max<int64_t>(clen, 64), 2048);
-    c->chunk_len = clen;
-    c->nchunk = (int)((c->N + clen - 1) / clen);
-    c->smem = (size_t)Rk * clen * xsz;
+    SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
+    int64_t want_blocks;
+    if (c->hmat) {
+        c->smem = (size_t)Rk * hmat::kChunk * xsz + (size_t)hmat::kMaxRank * Rk * sizeof(double);
+        c->nchunk = 0;
+        c->chunk_len = 0;
+        want_blocks = std::max<int64_t>(c->hops.n_tiles, c->hops.n_lr);
+    } else {
+        // column chunks of at most 2048 sources staged in shared memory per instance,
+        // enough (row block, chunk) tiles for >= 2 per SM
+        const int64_t rows_per_blk = (int64_t)kSimThreads * vec;
+        const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
+        int64_t want_chunks = std::max<int64_t>(1, (2LL * sms + nrb - 1) / nrb);
+        int64_t clen = (c->N + want_chunks - 1) / want_chunks;
+        clen = std::min<int64_t>(std::max<int64_t>(clen, 64), 2048);
+        c->chunk_len = clen;
+        c->nchunk = (int)((c->N + clen - 1) / clen);
+        c->smem = (size_t)Rk * clen * xsz;
+        want_blocks = nrb * c->nchunk;
+    }
     QDFN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
     int occ = 0;
     QDFN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kSimThreads, c->smem));
     if (occ < 1) return fail(QDFN_ERR_CUDA, "simulation kernel cannot be resident");
     const int64_t work_items = (int64_t)Rk * c->N;
-    int64_t nb = std::min<int64_t>((int64_t)sms * occ, std::max<int64_t>(1, nrb * c->nchunk));
-    nb = std::max<int64_t>(1, std::min<int64_t>(nb, (work_items + 31) / 32));
-    if (c->nblocks > 0) nb = std::min<int64_t>(nb, c->nblocks);
+    int64_t nb = std::min<int64_t>((int64_t)sms * occ, std::max<int64_t>(1, want_blocks));
+    nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>((work_items + 31) / 32, 1)));
+    if (c->nblocks_override > 0) nb = std::min<int64_t>(nb, c->nblocks_override);
     c->nblocks = (int)nb;
-    ApplyKernel ka = apply_kernel(c->prec, c->R);
-    QDFN_CUDA(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
-    // buffers sized by the launch shape
+    if (c->hmat) {
+        ApplyKernel a, b, rows;
+        if (c->prec == QDFN_FP64) hmat_apply_kernels<double>(Rk, &a, &b, &rows);
+        else hmat_apply_kernels<float>(Rk, &a, &b, &rows);
+        QDFN_CUDA(cudaFuncSetAttribute(a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+        QDFN_CUDA(cudaFuncSetAttribute(b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    } else {
+        ApplyKernel ka = apply_kernel(c->prec, c->R);
+        QDFN_CUDA(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    }
     c->release(c->part_s);
     c->release(c->part_n);
     c->release(c->red);
+    c->part_s = c->part_n = nullptr;
     int rc;
-    if ((rc = c->dalloc(&c->part_s, (size_t)c->nchunk * Rk * c->N))) return rc;
-    if ((rc = c->dalloc(&c->part_n, (size_t)c->nchunk * Rk * c->N))) return rc;
+    if (!c->hmat) {
+        if ((rc = c->dalloc(&c->part_s, (size_t)c->nchunk * Rk * c->N))) return rc;
+        if ((rc = c->dalloc(&c->part_n, (size_t)c->nchunk * Rk * c->N))) return rc;
+    }
     if ((rc = c->dalloc(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots))) return rc;
     return QDFN_OK;
 }
@@ -786,7 +871,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
-    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1);
+    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, 8);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
@@ -842,10 +927,13 @@ extern "C" int qdfn_ctx_destroy(qdfn_ctx* ctx) {
 
 namespace {
 
+void release_hmat(qdfn_ctx* c);
+
 // Converts FP64 Ks/Kn already on the device into the stored operator.
 int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t ld_in, int layout,
                      int precision, cudaStream_t st) {
     const int64_t N = c->N;
+    release_hmat(c);
     c->release(c->E);
     c->release(c->Kn);
     c->E = c->Kn = nullptr;
@@ -951,7 +1039,7 @@ extern "C" int qdfn_run_async(qdfn_ctx* c, int64_t nsteps, double timeout_s, voi
     QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, sizeof(int), st));
     QDFN_CUDA(cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), st));
     SimParams p = make_params(c, budget_ns);
-    SimKernel k = sim_kernel(c->prec, c->R);
+    SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
     void* args[] = {&p, &nsteps};
     QDFN_CUDA(cudaLaunchCooperativeKernel((const void*)k, dim3(c->nblocks), dim3(kSimThreads), args,
                                           c->smem, st));
@@ -982,6 +1070,14 @@ extern "C" int qdfn_run(qdfn_ctx* c, int64_t nsteps, double timeout_s) {
 }
 
 extern "C" int qdfn_kernels_per_run(const qdfn_ctx* c) { return c ? 1 : 0; }
+
+extern "C" int qdfn_get_counters(const qdfn_ctx* c, int64_t* out, int n) {
+    if (!c || !out || n < 0) return fail(QDFN_ERR_INVALID, "null argument");
+    unsigned long long v[8];
+    QDFN_CUDA(cudaMemcpy(v, c->prof, sizeof(v), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n && k < 8; ++k) out[k] = (int64_t)v[k];
+    return QDFN_OK;
+}
 
 extern "C" int qdfn_get_state(const qdfn_ctx* c, int inst, double* V, double* D, double* theta,
                               double* friction, double* accel, double* sigma_old, double* T,
@@ -1047,11 +1143,23 @@ extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, do
     QDFN_CUDA(cudaMemcpy(saved.data(), c->D, n, cudaMemcpyDeviceToHost));
     QDFN_CUDA(cudaMemcpy(c->D, D, n, cudaMemcpyHostToDevice));
     SimParams p = make_params(c, 0);
-    apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
-    QDFN_CUDA(cudaGetLastError());
-    const int64_t tot = (int64_t)c->R * c->N;
-    k_chunk_reduce<<<(unsigned)((tot + 255) / 256), 256>>>(p);
-    QDFN_CUDA(cudaGetLastError());
+    const int64_t tot = (int64_t)kernel_R(c->R) * c->N;
+    if (c->hmat) {
+        ApplyKernel a, b, rows;
+        if (c->prec == QDFN_FP64) hmat_apply_kernels<double>(kernel_R(c->R), &a, &b, &rows);
+        else hmat_apply_kernels<float>(kernel_R(c->R), &a, &b, &rows);
+        a<<<c->nblocks, kSimThreads, c->smem>>>(p);
+        QDFN_CUDA(cudaGetLastError());
+        b<<<c->nblocks, kSimThreads, c->smem>>>(p);
+        QDFN_CUDA(cudaGetLastError());
+        rows<<<(unsigned)((tot + 255) / 256), 256>>>(p);
+        QDFN_CUDA(cudaGetLastError());
+    } else {
+        apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
+        QDFN_CUDA(cudaGetLastError());
+        k_chunk_reduce<<<(unsigned)((tot + 255) / 256), 256>>>(p);
+        QDFN_CUDA(cudaGetLastError());
+    }
     QDFN_CUDA(cudaDeviceSynchronize());
     QDFN_CUDA(cudaMemcpy(tld, c->tld, n, cudaMemcpyDeviceToHost));
     QDFN_CUDA(cudaMemcpy(knd, c->knd, n, cudaMemcpyDeviceToHost));
@@ -1066,12 +1174,174 @@ extern "C" int qdfn_get_kself(const qdfn_ctx* c, double* kself) {
     return QDFN_OK;
 }
 
+namespace {
+
+template <class T>
+void put(std::vector<unsigned char>& buf, size_t off_elems, double v) {
+    reinterpret_cast<T*>(buf.data())[off_elems] = (T)v;
+}
+
+void release_hmat(qdfn_ctx* c) {
+    for (void* q : c->hbufs) c->release(q);
+    c->hbufs.clear();
+    c->hops = hmat::Ops{};
+}
+
+template <class T>
+int dcopy(qdfn_ctx* c, const T* src, size_t n, T** dst) {
+    int rc = c->dalloc(dst, n);
+    if (rc) return rc;
+    c->hbufs.push_back(*dst);
+    if (n) QDFN_CUDA(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return QDFN_OK;
+}
+
+}  // namespace
+
 extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, const int64_t* rank_s,
                                 const double* const* U_s, const double* const* Vt_s,
                                 const double* const* D_s, const int64_t* rank_n,
                                 const double* const* U_n, const double* const* Vt_n,
                                 const double* const* D_n, int precision) {
-    (void)c; (void)nb; (void)range; (void)rank_s; (void)U_s; (void)Vt_s; (void)D_s;
-    (void)rank_n; (void)U_n; (void)Vt_n; (void)D_n; (void)precision;
-    return fail(QDFN_ERR_STATE, "H-matrix operator not available in this build");
+    if (!c || !range || !rank_s || !rank_n) return fail(QDFN_ERR_INVALID, "null argument");
+    if (nb < 1) return fail(QDFN_ERR_INVALID, "nb must be >= 1");
+    if (precision != QDFN_FP64 && precision != QDFN_FP32)
+        return fail(QDFN_ERR_INVALID, "H-matrix blocks are stored in QDFN_FP64 or QDFN_FP32");
+    const int64_t N = c->N;
+    const int Rk = kernel_R(c->R);
+    const size_t esz = precision == QDFN_FP64 ? 8 : 4;
+    // validate and lay out
+    std::vector<hmat::Blk> blk(2 * nb);
+    size_t store = 0;
+    int64_t toff = 0, slot = 0;
+    std::vector<double> kself(N, 0.0);
+    for (int side = 0; side < 2; ++side) {
+        const int64_t* rank = side == 0 ? rank_s : rank_n;
+        const double* const* U = side == 0 ? U_s : U_n;
+        const double* const* Vt = side == 0 ? Vt_s : Vt_n;
+        const double* const* Dm = side == 0 ? D_s : D_n;
+        for (int64_t b = 0; b < nb; ++b) {
+            const int64_t s0 = range[4 * b], s1 = range[4 * b + 1], r0 = range[4 * b + 2], r1 = range[4 * b + 3];
+            if (s0 < 0 || r0 < 0 || s1 < s0 || r1 < r0 || s1 >= N || r1 >= N)
+                return fail(QDFN_ERR_INVALID, "block range out of [0, N)");
+            hmat::Blk& B = blk[side * nb + b];
+            B.s0 = s0; B.ns = s1 - s0 + 1; B.r0 = r0; B.nr = r1 - r0 + 1;
+            if (B.nr > ((int64_t)1 << 20) * hmat::kTileRows) return fail(QDFN_ERR_INVALID, "block too tall");
+            B.slot = slot;
+            slot += B.nr;
+            if (rank[b] < 0) {
+                if (!Dm || !Dm[b]) return fail(QDFN_ERR_INVALID, "dense block without data");
+                B.rank = -1;
+                B.off_a = (int64_t)store;
+                store += (size_t)B.ns * B.nr;
+                B.off_b = 0; B.toff = 0;
+            } else {
+                if (rank[b] > hmat::kMaxRank) return fail(QDFN_ERR_INVALID, "low-rank block rank above 128");
+                if (!U || !Vt || (rank[b] > 0 && (!U[b] || !Vt[b])))
+                    return fail(QDFN_ERR_INVALID, "low-rank block without factors");
+                if (s0 == r0 && s1 == r1 && side == 0)
+                    return fail(QDFN_ERR_INVALID, "diagonal shear block must be dense (K_Self)");
+                B.rank = (int32_t)rank[b];
+                B.off_a = (int64_t)store;
+                store += (size_t)B.rank * B.ns;
+                B.off_b = (int64_t)store;
+                store += (size_t)B.rank * B.nr;
+                B.toff = toff;
+                toff += B.rank;
+            }
+        }
+    }
+    // pack (converted to the storage type); the shear diagonal is zeroed and
+    // K_Self = -K_ii taken from it (StiffnessTransitionToLoading)
+    std::vector<unsigned char> hbuf(store * esz + 16);
+    auto putv = [&](size_t o, double v) {
+        if (esz == 8) put<double>(hbuf, o, v); else put<float>(hbuf, o, v);
+    };
+    for (int side = 0; side < 2; ++side) {
+        const double* const* U = side == 0 ? U_s : U_n;
+        const double* const* Vt = side == 0 ? Vt_s : Vt_n;
+        const double* const* Dm = side == 0 ? D_s : D_n;
+        for (int64_t b = 0; b < nb; ++b) {
+            const hmat::Blk& B = blk[side * nb + b];
+            if (B.rank < 0) {
+                const bool diag = side == 0 && B.s0 == B.r0 && B.ns == B.nr;
+                for (int64_t i = 0; i < B.nr; ++i)
+                    for (int64_t j = 0; j < B.ns; ++j) {
+                        double v = Dm[b][i * B.ns + j];
+                        if (diag && i == j) { kself[B.r0 + i] = -v; v = 0.0; }
+                        putv(B.off_a + j * B.nr + i, v);   // D^T
+                    }
+            } else {
+                for (int64_t kk = 0; kk < B.rank; ++kk) {
+                    for (int64_t j = 0; j < B.ns; ++j) putv(B.off_a + kk * B.ns + j, Vt[b][kk * B.ns + j]);
+                    for (int64_t i = 0; i < B.nr; ++i) putv(B.off_b + kk * B.nr + i, U[b][i * B.rank + kk]);
+                }
+            }
+        }
+    }
+    // receiver-row CSR of partial slots, block order, per side
+    std::vector<int64_t> rowptr(2 * (N + 1), 0), rowslot((size_t)slot);
+    for (int side = 0; side < 2; ++side) {
+        int64_t* rp = rowptr.data() + side * (N + 1);
+        for (int64_t b = 0; b < nb; ++b) {
+            const hmat::Blk& B = blk[side * nb + b];
+            for (int64_t i = 0; i < B.nr; ++i) rp[B.r0 + i + 1]++;
+        }
+        for (int64_t i = 0; i < N; ++i) rp[i + 1] += rp[i];
+    }
+    {
+        const int64_t base_n = rowptr[N];  // shear slots first in rowslot
+        std::vector<int64_t> fill(2 * N, 0);
+        for (int side = 0; side < 2; ++side) {
+            const int64_t* rp = rowptr.data() + side * (N + 1);
+            for (int64_t b = 0; b < nb; ++b) {
+                const hmat::Blk& B = blk[side * nb + b];
+                for (int64_t i = 0; i < B.nr; ++i) {
+                    const int64_t row = B.r0 + i;
+                    rowslot[(side ? base_n : 0) + rp[row] + fill[side * N + row]++] = B.slot + i;
+                }
+            }
+        }
+        // normal rows index rowslot from base_n: shift the normal CSR
+        for (int64_t i = 0; i <= N; ++i) rowptr[(N + 1) + i] += base_n;
+    }
+    std::vector<int64_t> lr, tiles;
+    for (int64_t q = 0; q < 2 * nb; ++q) {
+        if (blk[q].rank >= 0 && blk[q].rank > 0) lr.push_back(q);
+        const int64_t nt = (blk[q].nr + hmat::kTileRows - 1) / hmat::kTileRows;
+        for (int64_t t = 0; t < nt; ++t) tiles.push_back((q << 20) | t);
+    }
+    // device copies
+    release_hmat(c);
+    c->release(c->E); c->release(c->Kn);
+    c->E = c->Kn = nullptr;
+    int rc;
+    hmat::Blk* dblk; unsigned char* dstore; int64_t *dlr, *dtiles, *drp, *drs; double *dt, *dpart;
+    if ((rc = dcopy(c, blk.data(), blk.size(), &dblk)) || (rc = dcopy(c, hbuf.data(), hbuf.size(), &dstore)) ||
+        (rc = dcopy(c, lr.data(), lr.size(), &dlr)) || (rc = dcopy(c, tiles.data(), tiles.size(), &dtiles)) ||
+        (rc = dcopy(c, rowptr.data(), rowptr.size(), &drp)) ||
+        (rc = dcopy(c, rowslot.data(), rowslot.size(), &drs)))
+        return rc;
+    if ((rc = c->dalloc(&dt, (size_t)std::max<int64_t>(toff, 1) * Rk))) return rc;
+    c->hbufs.push_back(dt);
+    if ((rc = c->dalloc(&dpart, (size_t)std::max<int64_t>(slot, 1) * Rk))) return rc;
+    c->hbufs.push_back(dpart);
+    hmat::Ops& h = c->hops;
+    h.blk = dblk; h.nb = nb; h.store = dstore; h.lr_list = dlr; h.n_lr = (int64_t)lr.size();
+    h.tile_list = dtiles; h.n_tiles = (int64_t)tiles.size(); h.t = dt; h.part = dpart;
+    h.rowptr = drp; h.rowslot = drs;
+    c->prec = precision;
+    c->hmat = 1;
+    c->ld = 0;
+    if ((rc = h2d(c->kself, kself.data(), N * 8))) return rc;
+    // Omega = sqrt(K_Self / Mass) (Main_H :72)
+    std::vector<double> m((size_t)Rk * N), om(m.size());
+    QDFN_CUDA(cudaMemcpy(m.data(), c->mass, m.size() * 8, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < m.size(); ++q) {
+        const double x = kself[q % N] / m[q];
+        if (x < 0) return fail(QDFN_ERR_DOMAIN, "sqrt of a negative number in Omega (K_ii > 0)");
+        om[q] = std::sqrt(x);
+    }
+    if ((rc = h2d(c->omega, om.data(), om.size() * 8))) return rc;
+    return configure_launch(c);
 }

@@ -28,6 +28,7 @@ EXPORTS = [
     "qdfn_assemble_rect", "qdfn_assemble_rect_dev", "qdfn_assemble_tri", "qdfn_assemble_tri_dev",
     "qdfn_ctx_create", "qdfn_ctx_destroy", "qdfn_set_dense", "qdfn_set_dense_dev", "qdfn_set_hmatrix",
     "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
+    "qdfn_get_counters",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
 ]
 
@@ -87,6 +88,7 @@ def load():
     L.qdfn_run_async.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
     L.qdfn_sync.argtypes = [C.c_void_p]
     L.qdfn_kernels_per_run.argtypes = [C.c_void_p]
+    L.qdfn_get_counters.argtypes = [C.c_void_p, _ip, C.c_int]
     L.qdfn_get_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 8 + [_ip]
     L.qdfn_set_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [C.c_double, C.c_double, C.c_int64]
     L.qdfn_get_history.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [_ip]

@@ -1,0 +1,262 @@
+"""H-matrix elastic operator: cluster tree, block structure, compression.
+
+The reference builds its tree by recursive k-means bisection
+(scripts/Functions_Hmatrix.jl:1-158, `GroupAndSort_AllLevel`), declares a block
+admissible when centre distance / max diameter > 1 (:163-212, `BuildHierarchy`)
+and compresses admissible blocks with `LowRankApprox.pqrfact` of the full
+dense block (scripts/Functions_BuildInputFile.jl:705-712, 784-791).  Its
+k-means is randomly initialised, so its trees are not reproducible; here the
+tree is a deterministic principal-axis median bisection down to `leaf`
+patches, admissibility is the standard bounding-box rule
+max(diam) <= eta * dist, and admissible blocks are compressed by adaptive
+cross approximation with partial pivoting (ACA) followed by QR/SVD
+recompression, to a relative Frobenius tolerance.  Blocks are formed on the GPU
+by the assembly kernels; the block list is handed to qdfn_set_hmatrix in the
+reference's ElementRange_SR form (source range, receiver range).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+
+class ClusterTree:
+    """Binary tree over patch centres; `perm` orders patches so every node is a
+    contiguous index range [start, end)."""
+
+    def __init__(self, points, leaf=64):
+        pts = np.asarray(points, dtype=np.float64)
+        n = pts.shape[0]
+        self.leaf = leaf
+        self.starts, self.ends, self.children, self.lo, self.hi = [], [], [], [], []
+        perm = np.arange(n)
+
+        def build(idx, start):
+            node = len(self.starts)
+            self.starts.append(start)
+            self.ends.append(start + len(idx))
+            self.children.append(())
+            p = pts[idx]
+            self.lo.append(p.min(axis=0))
+            self.hi.append(p.max(axis=0))
+            if len(idx) <= leaf:
+                perm[start:start + len(idx)] = idx
+                return node
+            c = p - p.mean(axis=0)
+            # principal axis of the centres (deterministic sign)
+            w, v = np.linalg.eigh(c.T @ c)
+            ax = v[:, -1]
+            ax = ax if ax[np.argmax(np.abs(ax))] > 0 else -ax
+            proj = c @ ax
+            order = np.argsort(proj, kind="stable")
+            half = len(idx) // 2
+            a = build(idx[order[:half]], start)
+            b = build(idx[order[half:]], start + half)
+            self.children[node] = (a, b)
+            return node
+
+        build(np.arange(n), 0)
+        self.perm = perm
+        self.lo = np.array(self.lo)
+        self.hi = np.array(self.hi)
+
+    def diam(self, k):
+        return float(np.linalg.norm(self.hi[k] - self.lo[k]))
+
+    def dist(self, a, b):
+        gap = np.maximum(0.0, np.maximum(self.lo[a] - self.hi[b], self.lo[b] - self.hi[a]))
+        return float(np.linalg.norm(gap))
+
+
+def block_partition(tree, eta=2.0):
+    """(src_node, recv_node, admissible) leaves of the block tree."""
+    out = []
+
+    def rec(t, s):
+        if max(tree.diam(t), tree.diam(s)) <= eta * tree.dist(t, s):
+            out.append((s, t, True))
+            return
+        ct, cs = tree.children[t], tree.children[s]
+        if not ct and not cs:
+            out.append((s, t, False))
+            return
+        for a in (ct or (t,)):
+            for b in (cs or (s,)):
+                rec(a, b)
+
+    rec(0, 0)
+    return out
+
+
+def aca(block, tol, max_rank=None):
+    """ACA with partial pivoting on a dense torch block (m x n), then QR/SVD
+    recompression; returns (U (m x k), Vt (k x n)) with
+    ||block - U Vt||_F <= tol ||block||_F (estimated the ACA way)."""
+    import torch
+    m, n = block.shape
+    max_rank = max_rank or min(m, n)
+    Us, Vs = [], []
+    used_rows = torch.zeros(m, dtype=torch.bool, device=block.device)
+    i = 0
+    frob2 = 0.0
+    for _ in range(max_rank):
+        row = block[i].clone()
+        for u, v in zip(Us, Vs):
+            row -= u[i] * v
+        used_rows[i] = True
+        j = int(torch.argmax(torch.abs(row)))
+        piv = row[j]
+        if abs(float(piv)) == 0.0:
+            cand = torch.nonzero(~used_rows).flatten()
+            if len(cand) == 0:
+                break
+            i = int(cand[0])
+            continue
+        v = row / piv
+        col = block[:, j].clone()
+        for u, vv in zip(Us, Vs):
+            col -= vv[j] * u
+        u = col
+        nu2 = float(u @ u) * float(v @ v)
+        cross = 0.0
+        for uu, vv in zip(Us, Vs):
+            cross += float(uu @ u) * float(vv @ v)
+        frob2 += nu2 + 2 * cross
+        Us.append(u)
+        Vs.append(v)
+        if nu2 <= (tol ** 2) * max(frob2, 1e-300):
+            break
+        cand = torch.abs(u).masked_fill(used_rows, -1.0)
+        i = int(torch.argmax(cand))
+        if cand[i] < 0:
+            break
+    if not Us:
+        return (torch.zeros((m, 0), dtype=block.dtype, device=block.device),
+                torch.zeros((0, n), dtype=block.dtype, device=block.device))
+    U = torch.stack(Us, dim=1)
+    V = torch.stack(Vs, dim=0)
+    # recompression: U = Qu Ru, V^T = Qv Rv -> SVD of Ru Rv^T
+    Qu, Ru = torch.linalg.qr(U)
+    Qv, Rv = torch.linalg.qr(V.T)
+    W, S, Zt = torch.linalg.svd(Ru @ Rv.T)
+    tot = float(torch.sum(S ** 2))
+    tail = torch.flip(torch.cumsum(torch.flip(S ** 2, [0]), 0), [0])
+    keep = int(torch.sum(tail > (tol ** 2) * tot))
+    keep = max(keep, 1)
+    U2 = Qu @ (W[:, :keep] * S[:keep])
+    Vt2 = (Zt[:keep] @ Qv.T)
+    return U2, Vt2
+
+
+class HMatrix:
+    """Blocks of one operator pair (shear, normal) over a ClusterTree ordering."""
+
+    def __init__(self, ranges, dense_s, U_s, Vt_s, dense_n, U_n, Vt_n, perm):
+        self.ranges = ranges          # nb x 4: src_begin, src_end, recv_begin, recv_end (0-based, inclusive)
+        self.dense_s, self.U_s, self.Vt_s = dense_s, U_s, Vt_s
+        self.dense_n, self.U_n, self.Vt_n = dense_n, U_n, Vt_n
+        self.perm = perm
+
+    @property
+    def nblocks(self):
+        return self.ranges.shape[0]
+
+    def stored_entries(self):
+        tot = 0
+        for b in range(self.nblocks):
+            for D, U, Vt in ((self.dense_s[b], self.U_s[b], self.Vt_s[b]), (self.dense_n[b], self.U_n[b],
+                                                                             self.Vt_n[b])):
+                tot += D.size if D is not None else U.size + Vt.size
+        return tot
+
+    def to_dense(self, N):
+        Ks, Kn = np.zeros((N, N)), np.zeros((N, N))
+        for b, (s0, s1, r0, r1) in enumerate(self.ranges):
+            for K, D, U, Vt in ((Ks, self.dense_s[b], self.U_s[b], self.Vt_s[b]),
+                                (Kn, self.dense_n[b], self.U_n[b], self.Vt_n[b])):
+                K[r0:r1 + 1, s0:s1 + 1] = D if D is not None else U @ Vt
+        return Ks, Kn
+
+
+def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, device="cuda"):
+    """Build the H-matrix of a rectangular-patch system (records n x 8).
+    Returns (HMatrix, perm): block ranges index the permuted ordering
+    records[perm]."""
+    import torch
+    from . import assemble
+    tree = ClusterTree(np.asarray(records)[:, :3] * np.array([1.0, 1.0, -1.0]), leaf=leaf)
+    perm = tree.perm
+    rec = torch.tensor(np.ascontiguousarray(np.asarray(records)[perm]), dtype=torch.float64, device=device)
+    blocks = block_partition(tree, eta)
+    ranges, ds, us, vs, dn, un, vn = [], [], [], [], [], [], []
+    for (s, t, adm) in blocks:
+        s0, s1 = tree.starts[s], tree.ends[s]
+        r0, r1 = tree.starts[t], tree.ends[t]
+        ns, nr = s1 - s0, r1 - r0
+        Ks = torch.empty((ns, nr), dtype=torch.float64, device=device)
+        Kn = torch.empty((ns, nr), dtype=torch.float64, device=device)
+        assemble.assemble_rect_dev(rec[s0:s1], rec[r0:r1], shear_modulus, poisson, Ks, Kn, layout="col")
+        Bs, Bn = Ks.T, Kn.T      # recv x src
+        ranges.append((s0, s1 - 1, r0, r1 - 1))
+        if adm:
+            for B, Ul, Vl, Dl in ((Bs, us, vs, ds), (Bn, un, vn, dn)):
+                U, Vt = aca(B.contiguous(), tol)
+                if U.shape[1] * (nr + ns) < nr * ns:
+                    Ul.append(U.cpu().numpy()); Vl.append(Vt.cpu().numpy()); Dl.append(None)
+                else:
+                    Ul.append(None); Vl.append(None); Dl.append(B.cpu().numpy())
+        else:
+            for B, Ul, Vl, Dl in ((Bs, us, vs, ds), (Bn, un, vn, dn)):
+                Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
+    return HMatrix(np.array(ranges, dtype=np.int64), ds, us, vs, dn, un, vn, perm), perm
+
+
+def set_hmatrix(sim, H, precision="fp64"):
+    """Hand an HMatrix to a Simulation (qdfn_set_hmatrix)."""
+    L = _lib.load()
+    nb = H.nblocks
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    keep = []
+
+    def arr(a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def plist(lst):
+        p = (C.POINTER(C.c_double) * nb)()
+        for b, a in enumerate(lst):
+            p[b] = arr(a) if a is not None else C.POINTER(C.c_double)()
+        return p
+
+    rng = np.ascontiguousarray(H.ranges, dtype=np.int64)
+    rank_s = np.array([-1 if H.dense_s[b] is not None else H.U_s[b].shape[1] for b in range(nb)], dtype=np.int64)
+    rank_n = np.array([-1 if H.dense_n[b] is not None else H.U_n[b].shape[1] for b in range(nb)], dtype=np.int64)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+    _lib.check(L.qdfn_set_hmatrix(sim._h, nb, ip(rng), ip(rank_s), plist(H.U_s), plist(H.Vt_s), plist(H.dense_s),
+                                  ip(rank_n), plist(H.U_n), plist(H.Vt_n), plist(H.dense_n), prec))
+    sim._keep["hmat"] = (keep, rng, rank_s, rank_n)
+
+
+def set_hmatrix_from_reference(sim, ElementRange_SR, ShearStiffness_H, NormalStiffness_H, zero_normal=False,
+                               precision="fp64"):
+    """Blocks in the reference's form: ElementRange_SR (B x 4, 1-based,
+    inclusive: source range, receiver range) and per block either a dense
+    (recv x src) matrix or a (U, Vt) pair (e.g. a PartialQR converted to
+    U = Q, Vt = R P^T)."""
+    rng = np.asarray(ElementRange_SR, dtype=np.int64) - 1
+    nb = rng.shape[0]
+    ds, us, vs, dn, un, vn = [], [], [], [], [], []
+    for b in range(nb):
+        for blk, Dl, Ul, Vl in ((ShearStiffness_H[b], ds, us, vs), (NormalStiffness_H[b], dn, un, vn)):
+            if zero_normal and Dl is dn:
+                nr, ns = rng[b, 3] - rng[b, 2] + 1, rng[b, 1] - rng[b, 0] + 1
+                Dl.append(np.zeros((nr, ns))); Ul.append(None); Vl.append(None)
+            elif isinstance(blk, (tuple, list)):
+                Ul.append(np.asarray(blk[0])); Vl.append(np.asarray(blk[1])); Dl.append(None)
+            else:
+                Dl.append(np.asarray(blk)); Ul.append(None); Vl.append(None)
+    H = HMatrix(rng, ds, us, vs, dn, un, vn, None)
+    set_hmatrix(sim, H, precision)
+    return H

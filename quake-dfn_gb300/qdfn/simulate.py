@@ -118,6 +118,14 @@ class Simulation:
     def kernels_per_run(self):
         return self.L.qdfn_kernels_per_run(self._h)
 
+    def counters(self):
+        """Cumulative device counters: ns in time control / operator / solves /
+        rotation, solve passes, steps."""
+        out = np.zeros(8, dtype=np.int64)
+        _lib.check(self.L.qdfn_get_counters(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)), 8))
+        keys = ("ns_control", "ns_operator", "ns_solve", "ns_rotate", "solve_passes", "steps")
+        return {k: int(out[i]) for i, k in enumerate(keys)}
+
     # -- state --------------------------------------------------------------
     def state(self, inst=0):
         N = self.N

@@ -1,0 +1,93 @@
+"""H-matrix operator: block structure (CPU) and the device operator and
+simulation against the oracle's H path and against the dense operator (GPU)."""
+import numpy as np
+import pytest
+
+from _systems import cols, mixed_rects, problem_for, small_network
+
+G, NU = 32e9, 0.25
+
+
+def test_cluster_tree_is_a_permutation_with_contiguous_nodes():
+    from qdfn.hmatrix import ClusterTree
+    pts = np.random.default_rng(0).uniform(-1000, 1000, (700, 3))
+    t = ClusterTree(pts, leaf=32)
+    assert sorted(t.perm.tolist()) == list(range(700))
+    for k, ch in enumerate(t.children):
+        if ch:
+            a, b = ch
+            assert t.starts[a] == t.starts[k] and t.ends[a] == t.starts[b] and t.ends[b] == t.ends[k]
+        else:
+            assert t.ends[k] - t.starts[k] <= 32
+
+
+def test_block_partition_covers_the_matrix_once():
+    from qdfn.hmatrix import ClusterTree, block_partition
+    pts = np.random.default_rng(1).uniform(-5000, 5000, (500, 3))
+    t = ClusterTree(pts, leaf=24)
+    cover = np.zeros((500, 500), dtype=int)
+    nadm = 0
+    for s, r, adm in block_partition(t, eta=2.0):
+        cover[t.starts[r]:t.ends[r], t.starts[s]:t.ends[s]] += 1
+        nadm += adm
+        if adm:
+            assert max(t.diam(s), t.diam(r)) <= 2.0 * t.dist(s, r)
+    assert np.all(cover == 1)
+    assert nadm > 0
+
+
+@pytest.mark.gpu
+def test_hmatrix_operator_matches_dense_and_oracle(qdfn_mod, oracle_mod):
+    from qdfn import assemble, hmatrix, simulate, synth
+    sysd = small_network(seed=5, n_faults=6, patch=250.0)
+    rec = sysd["records"]
+    H, perm = hmatrix.build_rect(rec, G, NU, leaf=32, eta=2.0, tol=1e-8)
+    recp = rec[perm]
+    N = rec.shape[0]
+    assert H.stored_entries() < 2 * N * N
+    Ks, Kn = assemble.assemble_rect(recp, recp, G, NU)
+    Hs, Hn = H.to_dense(N)
+    assert np.linalg.norm(Hs - Ks) < 1e-7 * np.linalg.norm(Ks)
+    assert np.linalg.norm(Hn - Kn) < 1e-7 * np.linalg.norm(Ks)
+    prob = problem_for(recp, Ks)
+    prob["interp_at_told"] = 1
+    sim = simulate.Simulation(prob)
+    hmatrix.set_hmatrix(sim, H, "fp64")
+    D = np.random.default_rng(2).uniform(0, 1, N)
+    tld, knd = sim.apply(D)
+    blocks = dict(range=H.ranges, sD=H.dense_s, sU=H.U_s, sVt=H.Vt_s, nD=H.dense_n, nU=H.U_n, nVt=H.Vt_n)
+    o = oracle_mod.Simulation(dict(prob), ("hmat", blocks))
+    otld, oknd = o.apply(D)
+    rel = lambda a, b: np.max(np.abs(a - b)) / np.max(np.abs(b))
+    assert rel(tld[0], otld) < 1e-12 and rel(knd[0], oknd) < 1e-12
+    assert np.allclose(sim.kself(), o.kself(), rtol=0, atol=0)
+    # against the dense operator: main_H divides after the product, main before
+    od = oracle_mod.Simulation(dict(prob), ("dense", Ks, Kn))
+    dt, dk = od.apply(D)
+    assert rel(tld[0], dt) < 1e-6 and rel(knd[0], dk) < 1e-6
+
+
+@pytest.mark.gpu
+def test_hmatrix_trajectory_matches_oracle(qdfn_mod, oracle_mod):
+    from qdfn import hmatrix, simulate, synth
+    sysd = small_network(seed=5, n_faults=6, patch=250.0)
+    rec = sysd["records"]
+    H, perm = hmatrix.build_rect(rec, G, NU, leaf=32, eta=2.0, tol=1e-8)
+    recp = rec[perm]
+    Hs, _ = H.to_dense(rec.shape[0])
+    prob = problem_for(recp, Hs)
+    prob["interp_at_told"] = 1
+    ext = synth.external_ramp(rec.shape[0], 1e6, 1e11)
+    for prec, tol in (("fp64", 1e-9), ("fp32", 1e-4)):
+        sim = simulate.Simulation(prob)
+        hmatrix.set_hmatrix(sim, H, prec)
+        sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+        sim.run(200, timeout_s=120)
+        blocks = dict(range=H.ranges, sD=H.dense_s, sU=H.U_s, sVt=H.Vt_s, nD=H.dense_n, nU=H.U_n, nVt=H.Vt_n)
+        o = oracle_mod.Simulation(dict(prob, ext_t=ext["t"], ext_n=ext["normal"], ext_s=ext["shear"],
+                                       ext_p=ext["pressure"]), ("hmat", blocks))
+        o.run(200)
+        st = sim.state(0)
+        assert st["step"] == 200
+        assert abs(st["T"] / o.T - 1) < tol
+        assert np.max(np.abs(st["D"] - o.state["D"])) / np.max(np.abs(o.state["D"])) < tol
