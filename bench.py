@@ -40,6 +40,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "quake-dfn_gb300"))
 
 YEAR = 365.25 * 24 * 3600.0
+TIMEOUT = 300.0   # bound on every device run (s): the kernel returns QDFN_ERR_TIMEOUT past it
 
 
 def parse():
@@ -204,13 +205,11 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu:
         Ks_host = Ks.cpu().numpy()  # (src, recv) memory = K[recv, src] column-major -> transpose view
         Kn_host = Kn.cpu().numpy()
-    del Ks, Kn
-    torch.cuda.empty_cache()
 
     # warm-up (untimed): the first W steps of the trajectory
-    sim.run(args.warmup)
+    sim.run(args.warmup, timeout_s=TIMEOUT)
     if sim64 is not None:
-        sim64.run(args.warmup)
+        sim64.run(args.warmup, timeout_s=TIMEOUT)
     start_states = [sim.state(r) for r in range(R)]
     T0 = np.array([s["T"] for s in start_states])
 
@@ -224,7 +223,7 @@ def run_ours(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     cnt0 = sim.counters()
-    sim.run_async(args.steps, stream=stream.cuda_stream)
+    sim.run_async(args.steps, stream=stream.cuda_stream, timeout_s=TIMEOUT)
     ev1.record(stream)
     torch.cuda.synchronize()
     sim.sync()
@@ -268,7 +267,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
-        sim64.run_async(args.steps, stream=stream.cuda_stream)
+        sim64.run_async(args.steps, stream=stream.cuda_stream, timeout_s=TIMEOUT)
         f1.record(stream)
         torch.cuda.synchronize()
         sim64.sync()
@@ -278,6 +277,40 @@ def run_ours(args):
         slip_err = float(np.max(np.abs(end_state0["D"] - s1["D"])) / max(np.max(np.abs(s1["D"])), 1e-300))
         fp64 = {"value": yrs64 / (ms64 / 1e3 / 3600.0), "ms_per_step": ms64 / args.steps, "instances": 1,
                 "slip_rel_err_vs_fp64": slip_err, "mixed_over_fp64": (value / max(ws, 1)) / (yrs64 / (ms64 / 3.6e6))}
+
+    # ---- accuracy horizon: mixed ensemble vs the FP64 path from t = 0,
+    # compared every 100 steps (this network is chaotic: even a 1e-15
+    # perturbation of the FP64 operator grows to ~1e-6 slip error within ~2000
+    # steps, so the 1e-6 bar holds over a horizon, reported here)
+    horizon = None
+    if sim64 is not None:
+        pm = problem(sysd, draws, kdiag, R)
+        p1 = problem(sysd, {k: v[:N] for k, v in draws.items()}, kdiag, 1)
+        am = simulate.Simulation(pm, n_inst=R)
+        am.set_dense_device(Ks, Kn, args.precision, layout="col", stream=stream.cuda_stream)
+        a64 = simulate.Simulation(p1, n_inst=1)
+        a64.set_dense_device(Ks, Kn, "fp64", layout="col", stream=stream.cuda_stream)
+        for a in (am, a64):
+            a.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+        errs = []
+        done = 0
+        total = args.warmup + args.steps
+        while done < total:
+            n = min(100, total - done)
+            am.run(n, timeout_s=TIMEOUT)
+            a64.run(n, timeout_s=TIMEOUT)
+            done += n
+            d0, d1 = am.state(0)["D"], a64.state(0)["D"]
+            errs.append((done, float(np.max(np.abs(d0 - d1)) / max(np.max(np.abs(d1)), 1e-300))))
+        within = [st for st, e in errs if e <= 1e-6]
+        first_bad = next((st for st, e in errs if e > 1e-6), None)
+        horizon = {"checked_every": 100, "steps_within_1e-6": (first_bad - 100) if first_bad else total,
+                   "first_step_above_1e-6": first_bad,
+                   "err_at": {str(st): e for st, e in errs[::4] + [errs[-1]]}}
+        am.close()
+        a64.close()
+    del Ks, Kn
+    torch.cuda.empty_cache()
 
     # ---- e2e through the C ABI with host buffers, same window
     e2e = None
@@ -301,7 +334,7 @@ def run_ours(args):
             for r in range(R):
                 _lib.check(L.qdfn_set_state(sim._h, r, *(P(pin[k][r]) for k in names), Ts[r].value, dts[r].value,
                                             steps[r].value))
-            _lib.check(L.qdfn_run(sim._h, 1, 0.0))
+            _lib.check(L.qdfn_run(sim._h, 1, TIMEOUT))
             for r in range(R):
                 _lib.check(L.qdfn_get_state(sim._h, r, *(P(pin[k][r]) for k in names), C.byref(Ts[r]),
                                             C.byref(dts[r]), C.byref(steps[r])))
@@ -337,6 +370,7 @@ def run_ours(args):
                                  "state vectors); peak %s" % (esz, peak_kind)},
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
+            "accuracy_horizon": horizon,
             "assembly": {"pairs": N * N, "ms": asm_ms, "pairs_per_s": N * N / (asm_ms / 1e3)},
             "phases_ms_per_step": {"time_control": phases["ns_control"] / 1e6 / args.steps,
                                    "operator": phases["ns_operator"] / 1e6 / args.steps,

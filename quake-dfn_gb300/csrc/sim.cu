@@ -102,6 +102,7 @@ struct SimParams {
     // barrier + reductions
     unsigned *bar_count, *bar_gen;
     double* red;                     // [2][nblocks][R][kRedSlots]
+    unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
     int* gerr;
     uint64_t budget_ns;             // wall-time budget of this launch
     unsigned long long* prof;       // [8] cumulative counters (qdfn_get_counters)
@@ -167,6 +168,33 @@ __device__ void block_reduce(double (&v)[kMaxInst][K], const int (&ops)[K], int 
     __syncthreads();
 }
 
+// Reduce K fields of every CTA's partial for instance r (slot layout of
+// SimParams::red) across the grid: one warp, lanes stride over the CTAs, then
+// a shuffle tree.  Every lane returns the result.  min/max only: exact, so the
+// result does not depend on the order.
+template <int K>
+__device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, int R, int r,
+                                            const int (&ops)[K], double (&out)[K]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = ops[k] == 0 ? -INFINITY : INFINITY;
+    for (int b = lane; b < nblk; b += 32) {
+        const double* s = slots_base + ((int64_t)b * R + r) * kRedSlots;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double x = __ldcg(s + k);
+            out[k] = ops[k] == 0 ? fmax(out[k], x) : fmin(out[k], x);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_xor_sync(0xffffffffu, out[k], o);
+            out[k] = ops[k] == 0 ? fmax(out[k], y) : fmin(out[k], y);
+        }
+}
+
 // ---------------------------------------------------------------------------
 // P2: dense elastic operator.  Tile = (row block of kSimThreads*VEC receivers,
 // column chunk).  x = D staged in shared memory; both matrices read once for all
@@ -180,7 +208,15 @@ __device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
     const int64_t N = p.N;
     const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
     const int64_t ntiles = nrb * p.nchunk;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    __shared__ long long s_tile;
+    for (;;) {
+        // tiles are handed out by a global counter (reset once per step), so
+        // CTAs that drew cheap tiles take more; results do not depend on the
+        // assignment because every tile writes its own partial slot
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(p.tile_ctr, 1ull);
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= ntiles) break;
         const int64_t rb = tile % nrb, c = tile / nrb;
         const int64_t j0 = c * p.chunk_len;
         const int64_t j1 = min(N, j0 + p.chunk_len);
@@ -244,15 +280,15 @@ __device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
                     for (int r = 0; r < R; ++r)
 #pragma unroll
                         for (int v = 0; v < VEC; ++v) { fs[r][v] = 0.f; fn[r][v] = 0.f; }
-                    for (; j + 4 <= jend; j += 4) {
-                        float e[4][VEC], k[4][VEC];
+                    for (; j + 8 <= jend; j += 8) {
+                        float e[8][VEC], k[8][VEC];
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
+                        for (int u = 0; u < 8; ++u) {
                             M::load(p.E, base + (j + u) * p.ld, e[u]);
                             M::load(p.Kn, base + (j + u) * p.ld, k[u]);
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; ++u)
+                        for (int u = 0; u < 8; ++u)
 #pragma unroll
                             for (int r = 0; r < R; ++r) {
                                 const float x = xs[r * p.chunk_len + j + u];
@@ -363,17 +399,16 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
                     s[4] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
                 }
+                if (blockIdx.x == 0) atomicExch(p.tile_ctr, 0ull);  // last used before the previous barrier
             }
             if (!grid_barrier(p, deadline)) return;
-            if (threadIdx.x < R) {
-                const int r = threadIdx.x;
-                double vmax = -INFINITY, vnan = 0, dtmin = INFINITY, any = 0, late = 0;
-                for (int b = 0; b < (int)gridDim.x; ++b) {
-                    const double* s = red_slot(phase, b, r);
-                    vmax = fmax(vmax, __ldcg(s)); vnan = fmax(vnan, __ldcg(s + 1));
-                    dtmin = fmin(dtmin, __ldcg(s + 2)); any = fmax(any, __ldcg(s + 3));
-                    late = fmax(late, __ldcg(s + 4));
-                }
+            if ((threadIdx.x >> 5) < R) {
+                const int r = threadIdx.x >> 5;
+                const int ops[5] = {0, 0, 1, 0, 0};
+                double f[5];
+                grid_fields<5>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r, ops, f);
+                double vmax = f[0], vnan = f[1], dtmin = f[2], any = f[3], late = f[4];
+                if ((threadIdx.x & 31) == 0) {
                 if (late != 0) s_stop = 1;   // benign race: every writer stores 1
                 if (vnan != 0) vmax = NAN;
                 if (any == 0 && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
@@ -388,6 +423,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 else Dt = DtRef;
                 s_dt[r] = Dt;
                 s_done[r] = 0;
+                }
             }
             phase++;
             __syncthreads();
@@ -478,24 +514,26 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
                 }
             if (!grid_barrier(p, deadline)) return;
-            if (threadIdx.x < R) {
-                const int r = threadIdx.x;
+            if ((threadIdx.x >> 5) < R) {
+                const int r = threadIdx.x >> 5;
                 if (!s_done[r]) {
-                    double mflag = 1, mdt = INFINITY, any4 = 0, err = 0;
-                    for (int b = 0; b < (int)gridDim.x; ++b) {
-                        const double* s = red_slot(phase, b, r);
-                        mflag = fmin(mflag, __ldcg(s)); mdt = fmin(mdt, __ldcg(s + 1));
-                        any4 = fmax(any4, __ldcg(s + 2)); err = fmin(err, __ldcg(s + 3));
-                    }
-                    if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
-                    else if (mflag == 0) {
-                        s_dt[r] = any4 != 0 ? 1e-3 : mdt;
-                    } else {
-                        s_dt[r] = mdt;   // Main_D :262 Dt = minimum(Dt_All)
-                        s_done[r] = 1;
+                    const int ops[4] = {1, 1, 0, 1};
+                    double f[4];
+                    grid_fields<4>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r, ops,
+                                   f);
+                    const double mflag = f[0], mdt = f[1], any4 = f[2], err = f[3];
+                    if ((threadIdx.x & 31) == 0) {
+                        if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
+                        else if (mflag == 0) {
+                            s_dt[r] = any4 != 0 ? 1e-3 : mdt;
+                        } else {
+                            s_dt[r] = mdt;   // Main_D :262 Dt = minimum(Dt_All)
+                            s_done[r] = 1;
+                        }
                     }
                 }
             }
+            __syncthreads();
             phase++;
             n_iter++;
             if (threadIdx.x == 0) s_iter++;
@@ -676,6 +714,7 @@ struct qdfn_ctx {
     double* red = nullptr;
     int* gerr;
     unsigned long long* prof;
+    unsigned long long* tile_ctr;
     void* E = nullptr;
     void* Kn = nullptr;
     int64_t n_ext = 0;
@@ -740,6 +779,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
     p.prof = c->prof;
+    p.tile_ctr = c->tile_ctr;
     p.h = c->hops;
     p.budget_ns = budget_ns;
     return p;
@@ -802,9 +842,9 @@ int configure_launch(qdfn_ctx* c) {
         // enough (row block, chunk) tiles for >= 2 per SM
         const int64_t rows_per_blk = (int64_t)kSimThreads * vec;
         const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
-        int64_t want_chunks = std::max<int64_t>(1, (2LL * sms + nrb - 1) / nrb);
+        int64_t want_chunks = std::max<int64_t>(1, (6LL * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
-        clen = std::min<int64_t>(std::max<int64_t>(clen, 64), 2048);
+        clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), 2048) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
         c->smem = (size_t)Rk * clen * xsz;
@@ -871,7 +911,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
-    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, 8);
+    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, 8); A(tile_ctr, 1);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
@@ -1038,6 +1078,7 @@ extern "C" int qdfn_run_async(qdfn_ctx* c, int64_t nsteps, double timeout_s, voi
     cudaStream_t st = (cudaStream_t)stream;
     QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, sizeof(int), st));
     QDFN_CUDA(cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), st));
+    QDFN_CUDA(cudaMemsetAsync(c->tile_ctr, 0, sizeof(unsigned long long), st));
     SimParams p = make_params(c, budget_ns);
     SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
     void* args[] = {&p, &nsteps};
@@ -1155,6 +1196,7 @@ extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, do
         rows<<<(unsigned)((tot + 255) / 256), 256>>>(p);
         QDFN_CUDA(cudaGetLastError());
     } else {
+        QDFN_CUDA(cudaMemset(c->tile_ctr, 0, sizeof(unsigned long long)));
         apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
         QDFN_CUDA(cudaGetLastError());
         k_chunk_reduce<<<(unsigned)((tot + 255) / 256), 256>>>(p);
