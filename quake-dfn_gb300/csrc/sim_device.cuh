@@ -37,15 +37,31 @@ __device__ __forceinline__ double jlog(double x, int& err) {
     return log(x);
 }
 
+// The normal-stress coupling term alpha * dsigma / Dt / b / sigma of the aging
+// law is an exact (signed) zero when alpha == 0 and every operand is finite and
+// nonzero; adding it then leaves a nonzero sum unchanged, so it is skipped
+// (three FP64 divisions per call; Alpha_Evo is 0 in the reference,
+// QUAKEDFN_RunARG.jl:170).  Otherwise it is evaluated as written.
+__device__ __forceinline__ bool alpha_term_zero(double alpha, double Dt, double sig, double sig_old,
+                                                double b) {
+    return alpha == 0.0 && isfinite(Dt) && Dt != 0.0 && isfinite(sig) && sig != 0.0 &&
+           isfinite(sig_old) && isfinite(b) && b != 0.0;
+}
+
 __device__ __forceinline__ double evolution(double ThetaOld, double Dt, double V, double Dc,
                                             double alpha, double sig, double sig_old, double b,
                                             int fast, int dr, int& err) {
     if (dr == 1) {
+        const bool skip = alpha_term_zero(alpha, Dt, sig, sig_old, b);
         if (fast) {
-            const double Const_T = V / Dc + alpha * (sig - sig_old) / Dt / b / sig;
-            return (ThetaOld - 1 / Const_T) * exp(-V / Dc * Dt) + 1 / Const_T;
+            const double vd = V / Dc;
+            const double Const_T = (skip && vd != 0.0) ? vd : vd + alpha * (sig - sig_old) / Dt / b / sig;
+            // (-V)/Dc == -(V/Dc) exactly, so the quotient is reused
+            return (ThetaOld - 1 / Const_T) * exp(-vd * Dt) + 1 / Const_T;
         }
-        return (ThetaOld + Dt) / (1 + Dt * V / Dc + alpha * Dt * (sig - sig_old) / Dt / b / sig);
+        const double den0 = 1 + Dt * V / Dc;
+        const double den = (skip && den0 != 0.0) ? den0 : den0 + alpha * Dt * (sig - sig_old) / Dt / b / sig;
+        return (ThetaOld + Dt) / den;
     }
     return ThetaOld - V * ThetaOld / Dc * jlog(V * ThetaOld / Dc, err) * Dt;
 }
