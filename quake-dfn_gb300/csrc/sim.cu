@@ -38,29 +38,29 @@ constexpr int kRedSlots = 8;                // doubles per (CTA, instance) parti
 constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
 
 // ---------------------------------------------------------------------------
-// matrix element formats: each thread owns VEC consecutive receiver rows and
-// loads them with one 16-byte access per source column.
+// matrix element formats: each thread owns VEC consecutive receiver rows, one
+// 16-byte granule per source column (sload decodes it from shared memory).
 struct FmtF64 {
     static constexpr int VEC = 2;
     using X = double;  // staged x type
-    __device__ __forceinline__ static void load(const void* base, int64_t off, double v[2]) {
-        const double2 q = __ldg(reinterpret_cast<const double2*>(reinterpret_cast<const double*>(base) + off));
+    __device__ __forceinline__ static void sload(const unsigned char* p, double v[2]) {
+        const double2 q = *reinterpret_cast<const double2*>(p);
         v[0] = q.x; v[1] = q.y;
     }
 };
 struct FmtF32 {
     static constexpr int VEC = 4;
     using X = float;
-    __device__ __forceinline__ static void load(const void* base, int64_t off, float v[4]) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float*>(base) + off));
+    __device__ __forceinline__ static void sload(const unsigned char* p, float v[4]) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
         v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
     }
 };
 struct FmtBF16x2 {  // each 32-bit word: hi bf16 in the upper half, lo bf16 in the lower half
     static constexpr int VEC = 4;
     using X = float;
-    __device__ __forceinline__ static void load(const void* base, int64_t off, float v[4]) {
-        const uint4 q = __ldg(reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(base) + off));
+    __device__ __forceinline__ static void sload(const unsigned char* p, float v[4]) {
+        const uint4 q = *reinterpret_cast<const uint4*>(p);
         const uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -196,18 +196,94 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 }
 
 // ---------------------------------------------------------------------------
-// P2: dense elastic operator.  Tile = (row block of kSimThreads*VEC receivers,
-// column chunk).  x = D staged in shared memory; both matrices read once for all
-// R instances.  FP32 products are summed in FP32 over 32 columns, then folded
-// into FP64 accumulators (FP64 formats accumulate in FP64 directly).
+// P2: dense elastic operator.
+//
+// Storage is source-major: entry (receiver i, source j) at j*ld + i, so one
+// source column of a row block of kSimThreads*VEC receivers is a contiguous
+// 4 KB segment.  A tile is (row block, chunk of source columns); tiles are
+// handed out by a global counter.  Both matrices stream through a
+// kStages-deep ring of shared-memory stages filled by 1-D TMA bulk copies
+// (cp.async.bulk ... mbarrier::complete_tx) issued by one thread, so the bytes
+// in flight do not depend on the register-limited warp count of the
+// persistent kernel.  x = D (all R instances) is staged per tile.  FP32/BF16
+// products are summed in FP32 over 32 columns and folded into FP64
+// accumulators; FP64 storage accumulates in FP64.
+constexpr int kStages = 4;
+constexpr int kColsPerStage = 4;
+constexpr int kSegBytes = kSimThreads * 16;                     // one column of a row block
+constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn
+constexpr int kPipeBytes = kStages * kStageBytes;               // 128 KB
+constexpr int kMbarBytes = 128;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;                // 2 s per stage wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+    return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(m))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait on a stage; false when the limit passes
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(m, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(m, parity))
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    return true;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// pipeline state of one CTA: stage memory, its mbarriers and the number of
+// stage fills consumed so far (identical in every thread of the CTA)
+struct Pipe {
+    unsigned char* stages;
+    uint64_t* mbar;
+    uint32_t consumed;
+};
+
+__device__ __forceinline__ void pipe_init(Pipe& pp, unsigned char* smem) {
+    pp.stages = smem;
+    pp.mbar = reinterpret_cast<uint64_t*>(smem + kPipeBytes);
+    pp.consumed = 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(pp.mbar + s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+}
+
 template <class M, int R>
-__device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
+__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
+    constexpr int EB = 16 / VEC;   // bytes per stored entry
     constexpr int64_t rows_per_blk = (int64_t)kSimThreads * VEC;
     const int64_t N = p.N;
     const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
     const int64_t ntiles = nrb * p.nchunk;
+    const unsigned char* Eb = reinterpret_cast<const unsigned char*>(p.E);
+    const unsigned char* Kb = reinterpret_cast<const unsigned char*>(p.Kn);
     __shared__ long long s_tile;
     for (;;) {
         // tiles are handed out by a global counter (reset once per step), so
@@ -219,109 +295,101 @@ __device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
         if (tile >= ntiles) break;
         const int64_t rb = tile % nrb, c = tile / nrb;
         const int64_t j0 = c * p.chunk_len;
-        const int64_t j1 = min(N, j0 + p.chunk_len);
-        const int64_t L = j1 - j0;
-        __syncthreads();
+        const int64_t L = min(N, j0 + p.chunk_len) - j0;
+        const int64_t r0 = rb * rows_per_blk;
+        const int64_t rows_valid = min(rows_per_blk, N - r0);
+        // copy size: whole 16-byte granules; the padding up to ld is zero-filled
+        const uint32_t seg = (uint32_t)((rows_valid * EB + 15) / 16 * 16);
+        const int nst = (int)((L + kColsPerStage - 1) / kColsPerStage);
+        const uint32_t base = pp.consumed;
+        auto fill = [&](int q) {   // thread 0 only
+            const int slot = (int)((base + q) % kStages);
+            uint64_t* m = pp.mbar + slot;
+            const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
+            mbar_expect_tx(m, 2u * nc * seg);
+            unsigned char* st = pp.stages + (size_t)slot * kStageBytes;
+            for (int cc = 0; cc < nc; ++cc) {
+                const int64_t off = ((j0 + (int64_t)q * kColsPerStage + cc) * p.ld + r0) * EB;
+                bulk_g2s(st + (size_t)cc * kSegBytes, Eb + off, seg, m);
+                bulk_g2s(st + (size_t)(kColsPerStage + cc) * kSegBytes, Kb + off, seg, m);
+            }
+        };
+        __syncthreads();   // previous tile's stage reads and partial writes are done
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            for (int q = 0; q < min(kStages, nst); ++q) fill(q);
+        }
         for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kSimThreads) {
             const int r = (int)(q / L);
             const int64_t j = q % L;
             xs[r * p.chunk_len + j] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
         }
         __syncthreads();
-        const int64_t i0 = rb * rows_per_blk + (int64_t)threadIdx.x * VEC;
-        if (i0 < N) {
-            double as[R][VEC], an[R][VEC];
+        const int64_t i0 = r0 + (int64_t)threadIdx.x * VEC;
+        double as[R][VEC], an[R][VEC];
+        X fs[R][VEC], fn[R][VEC];
 #pragma unroll
-            for (int r = 0; r < R; ++r)
+        for (int r = 0; r < R; ++r)
 #pragma unroll
-                for (int v = 0; v < VEC; ++v) { as[r][v] = 0.0; an[r][v] = 0.0; }
-            const int64_t base = j0 * p.ld + i0;
-            if constexpr (sizeof(X) == 8) {
-                int64_t j = 0;
-                for (; j + 4 <= L; j += 4) {
-                    double e[4][VEC], k[4][VEC];
+            for (int v = 0; v < VEC; ++v) { as[r][v] = 0.0; an[r][v] = 0.0; fs[r][v] = 0; fn[r][v] = 0; }
+        bool ok = true;
+        for (int q = 0; q < nst; ++q) {
+            const uint32_t n = base + q;
+            const int slot = (int)(n % kStages);
+            if (!mbar_wait(pp.mbar + slot, (n / kStages) & 1u, kWaitLimitNs)) { ok = false; break; }
+            const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
+            const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * 16;
+            if (i0 < N) {
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        M::load(p.E, base + (j + u) * p.ld, e[u]);
-                        M::load(p.Kn, base + (j + u) * p.ld, k[u]);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
+                for (int cc = 0; cc < kColsPerStage; ++cc) {
+                    if (cc < nc) {
+                        X e[VEC], k[VEC];
+                        M::sload(st + (size_t)cc * kSegBytes, e);
+                        M::sload(st + (size_t)(kColsPerStage + cc) * kSegBytes, k);
+                        const int64_t jj = (int64_t)q * kColsPerStage + cc;
 #pragma unroll
                         for (int r = 0; r < R; ++r) {
-                            const double x = xs[r * p.chunk_len + j + u];
+                            const X x = xs[r * p.chunk_len + jj];
 #pragma unroll
                             for (int v = 0; v < VEC; ++v) {
-                                as[r][v] = fma(e[u][v], x, as[r][v]);
-                                an[r][v] = fma(k[u][v], x, an[r][v]);
+                                fs[r][v] = fma(e[v], x, fs[r][v]);
+                                fn[r][v] = fma(k[v], x, fn[r][v]);
                             }
-                        }
-                }
-                for (; j < L; ++j) {
-                    double e[VEC], k[VEC];
-                    M::load(p.E, base + j * p.ld, e);
-                    M::load(p.Kn, base + j * p.ld, k);
-#pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const double x = xs[r * p.chunk_len + j];
-#pragma unroll
-                        for (int v = 0; v < VEC; ++v) {
-                            as[r][v] = fma(e[v], x, as[r][v]);
-                            an[r][v] = fma(k[v], x, an[r][v]);
                         }
                     }
                 }
-            } else {
-                int64_t j = 0;
-                while (j < L) {
-                    const int64_t jend = min(L, j + 32);
-                    float fs[R][VEC], fn[R][VEC];
-#pragma unroll
-                    for (int r = 0; r < R; ++r)
-#pragma unroll
-                        for (int v = 0; v < VEC; ++v) { fs[r][v] = 0.f; fn[r][v] = 0.f; }
-                    for (; j + 8 <= jend; j += 8) {
-                        float e[8][VEC], k[8][VEC];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            M::load(p.E, base + (j + u) * p.ld, e[u]);
-                            M::load(p.Kn, base + (j + u) * p.ld, k[u]);
-                        }
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-#pragma unroll
-                            for (int r = 0; r < R; ++r) {
-                                const float x = xs[r * p.chunk_len + j + u];
-#pragma unroll
-                                for (int v = 0; v < VEC; ++v) {
-                                    fs[r][v] = fmaf(e[u][v], x, fs[r][v]);
-                                    fn[r][v] = fmaf(k[u][v], x, fn[r][v]);
-                                }
-                            }
-                    }
-                    for (; j < jend; ++j) {
-                        float e[VEC], k[VEC];
-                        M::load(p.E, base + j * p.ld, e);
-                        M::load(p.Kn, base + j * p.ld, k);
-#pragma unroll
-                        for (int r = 0; r < R; ++r) {
-                            const float x = xs[r * p.chunk_len + j];
-#pragma unroll
-                            for (int v = 0; v < VEC; ++v) {
-                                fs[r][v] = fmaf(e[v], x, fs[r][v]);
-                                fn[r][v] = fmaf(k[v], x, fn[r][v]);
-                            }
-                        }
-                    }
+                if (sizeof(X) == 8 || (q & 7) == 7 || q == nst - 1) {
 #pragma unroll
                     for (int r = 0; r < R; ++r)
 #pragma unroll
                         for (int v = 0; v < VEC; ++v) {
                             as[r][v] += (double)fs[r][v];
                             an[r][v] += (double)fn[r][v];
+                            fs[r][v] = 0;
+                            fn[r][v] = 0;
                         }
                 }
             }
+            __syncthreads();   // every thread is done with this slot
+            if (threadIdx.x == 0 && q + kStages < nst) {
+                fence_proxy_async();
+                fill(q + kStages);
+            }
+        }
+        pp.consumed = base + nst;
+        if (!ok) {
+            // drain the fills this tile issued before giving up (bounded)
+            if (threadIdx.x == 0) {
+                atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+                for (int q = 0; q < nst; ++q) {
+                    const uint32_t n = base + q;
+                    mbar_wait(pp.mbar + (n % kStages), (n / kStages) & 1u, kWaitLimitNs);
+                }
+            }
+            __syncthreads();
+            return false;
+        }
+        if (i0 < N) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -335,14 +403,18 @@ __device__ void dense_matvec(const SimParams& p, typename M::X* xs) {
                 }
         }
     }
+    return true;
 }
 
 template <class M, int R, bool HM>
 __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nsteps) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     using X = typename M::X;
-    X* xs = reinterpret_cast<X*>(smem_raw);
+    // dense: [stage ring | mbarriers | x];  H-matrix: [x | rank accumulators]
+    X* xs = reinterpret_cast<X*>(HM ? smem_raw : smem_raw + kPipeBytes + kMbarBytes);
     double* hacc = reinterpret_cast<double*>(smem_raw + (size_t)R * hmat::kChunk * sizeof(X));
+    Pipe pipe;
+    if constexpr (!HM) pipe_init(pipe, smem_raw);
     __shared__ double s_T[kMaxInst], s_dt[kMaxInst];
     __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
     __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop;
@@ -438,7 +510,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (!grid_barrier(p, deadline)) return;
             hmat::pass_b<X, R>(p.h, p.D, N, xs);
         } else {
-            dense_matvec<M, R>(p, xs);
+            if (!dense_matvec<M, R>(p, pipe, xs)) return;
         }
         if (!grid_barrier(p, deadline)) return;
         lap(1);
@@ -606,9 +678,11 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
 // Operator-only kernel (qdfn_apply_operator): one pass of P2 + chunk reduction.
 template <class M, int R>
 __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     using X = typename M::X;
-    dense_matvec<M, R>(p, reinterpret_cast<X*>(smem_raw));
+    Pipe pipe;
+    pipe_init(pipe, smem_raw);
+    dense_matvec<M, R>(p, pipe, reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes));
 }
 
 template <class X, int R>
@@ -847,7 +921,7 @@ int configure_launch(qdfn_ctx* c) {
         clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), 2048) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
-        c->smem = (size_t)Rk * clen * xsz;
+        c->smem = (size_t)kPipeBytes + kMbarBytes + (size_t)Rk * clen * xsz;
         want_blocks = nrb * c->nchunk;
     }
     QDFN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
