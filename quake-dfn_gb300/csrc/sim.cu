@@ -208,11 +208,11 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 // persistent kernel.  x = D (all R instances) is staged per tile.  FP32/BF16
 // products are summed in FP32 over 32 columns and folded into FP64
 // accumulators; FP64 storage accumulates in FP64.
-constexpr int kStages = 4;
+constexpr int kStages = 6;
 constexpr int kColsPerStage = 4;
 constexpr int kSegBytes = kSimThreads * 16;                     // one column of a row block
 constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn
-constexpr int kPipeBytes = kStages * kStageBytes;               // 128 KB
+constexpr int kPipeBytes = kStages * kStageBytes;               // 192 KB
 constexpr int kMbarBytes = 128;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;                // 2 s per stage wait
 
@@ -918,7 +918,9 @@ int configure_launch(qdfn_ctx* c) {
         const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
         int64_t want_chunks = std::max<int64_t>(1, (6LL * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
-        clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), 2048) + 7) / 8 * 8;
+        // x staging (R x chunk x elem) shares the 227 KB with the 192 KB stage ring
+        const int64_t cmax = std::max<int64_t>(64, (int64_t)(30 * 1024) / (Rk * (int64_t)xsz));
+        clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), std::min<int64_t>(2048, cmax)) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
         c->smem = (size_t)kPipeBytes + kMbarBytes + (size_t)Rk * clen * xsz;
