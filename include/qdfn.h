@@ -204,6 +204,23 @@ int qdfn_apply_operator(qdfn_ctx* ctx, const double* D, double* tld, double* knd
 /* K_Self of the stored operator (length N). */
 int qdfn_get_kself(const qdfn_ctx* ctx, double* kself);
 
+/* ---- allocation-free operator -------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (device memory owned by another allocator such as a Julia CUDA.jl pool or a
+ * framework's caching allocator, or loops where allocation is not allowed):
+ * the same products as qdfn_apply_operator -- tld = (K_ij/K_ii, zero diagonal)
+ * * (0 - D) and knd = Kn * D, FP64 -- computed straight from caller-owned
+ * DEVICE matrices Ks, Kn in source-major layout (Julia's column-major
+ * K[recv, src]: entry (r, s) at s*ld + r) and device vectors D, tld, knd (length
+ * N), enqueued on `stream`.  Allocates nothing: its scratch is a fixed 2 MiB
+ * device array holding N <= 16384; larger N is rejected with QDFN_ERR_INVALID.
+ * The first call on each device looks up the array's device address (with that
+ * device current), so make that first call before any stream capture.  All
+ * calls on a device share the array: calls whose kernels overlap on the GPU
+ * (other streams or host threads) race and must not be issued. */
+int qdfn_apply_dense_noalloc(int64_t N, const double* Ks, const double* Kn, int64_t ld,
+                             const double* D, double* tld, double* knd, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,7 @@ EXPORTS = [
     "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
     "qdfn_get_counters",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
+    "qdfn_apply_dense_noalloc",
 ]
 
 
@@ -94,6 +95,8 @@ def load():
     L.qdfn_get_history.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [_ip]
     L.qdfn_apply_operator.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.qdfn_get_kself.argtypes = [C.c_void_p, _dp]
+    L.qdfn_apply_dense_noalloc.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]
     _lib = L
     return L
 

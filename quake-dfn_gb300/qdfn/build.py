@@ -27,6 +27,7 @@ UNITS = {
     "assemble_rect.cu": ["--fmad=false"],
     "assemble_tri.cu": ["--fmad=false"],
     "sim.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
 }
 
 
