@@ -249,8 +249,7 @@ def run_ours(args):
 
     # ---- roofline of the persistent kernel (dominant, and the only kernel of the run)
     esz = {"fp32": 4, "bf16x2": 4, "fp64": 8}[args.precision]
-    ld = (N + 31) // 32 * 32
-    mat_bytes = 2 * N * ld * esz
+    mat_bytes = 2 * N * N * esz      # shear + normal operator, padding rows not counted
     vec_bytes = R * N * 8 * 14       # state read/write + matvec partials, per step
     alg_bytes = args.steps * (mat_bytes + vec_bytes)
     achieved = alg_bytes / (ms / 1e3) / 1e9
@@ -366,7 +365,7 @@ def run_ours(args):
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "note": "k_sim persistent kernel, algorithmic bytes = K x (2 N ld x %d B operator + "
+                         "note": "k_sim persistent kernel, algorithmic bytes = K x (2 N^2 x %d B operator + "
                                  "state vectors); peak %s" % (esz, peak_kind)},
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,

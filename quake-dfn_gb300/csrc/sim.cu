@@ -198,20 +198,22 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 // ---------------------------------------------------------------------------
 // P2: dense elastic operator.
 //
-// Storage is source-major: entry (receiver i, source j) at j*ld + i, so one
-// source column of a row block of kSimThreads*VEC receivers is a contiguous
-// 4 KB segment.  A tile is (row block, chunk of source columns); tiles are
-// handed out by a global counter.  Both matrices stream through a
-// kStages-deep ring of shared-memory stages filled by 1-D TMA bulk copies
+// Storage is tile-contiguous: receivers in row blocks of kSimThreads*VEC (one
+// 16-byte granule per thread and source column, 4 KB per column), and within a
+// row block the source columns back to back (see k_convert).  A tile is (row
+// block, chunk of source columns); tiles are handed out by a global counter.
+// Both matrices stream through a kStages-deep ring of 64 KB shared-memory
+// stages, each filled by one 32 KB TMA bulk copy per matrix
 // (cp.async.bulk ... mbarrier::complete_tx) issued by one thread, so the bytes
 // in flight do not depend on the register-limited warp count of the
 // persistent kernel.  x = D (all R instances) is staged per tile.  FP32/BF16
 // products are summed in FP32 over 32 columns and folded into FP64
 // accumulators; FP64 storage accumulates in FP64.
-constexpr int kStages = 6;
-constexpr int kColsPerStage = 4;
+constexpr int kStages = 3;
+constexpr int kColsPerStage = 8;
+constexpr int kFoldStages = 32 / kColsPerStage;                 // FP32 sums span 32 columns
 constexpr int kSegBytes = kSimThreads * 16;                     // one column of a row block
-constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn
+constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn, 64 KB
 constexpr int kPipeBytes = kStages * kStageBytes;               // 192 KB
 constexpr int kMbarBytes = 128;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;                // 2 s per stage wait
@@ -254,23 +256,66 @@ __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// pipeline state of one CTA: stage memory, its mbarriers and the number of
-// stage fills consumed so far (identical in every thread of the CTA)
+__device__ __forceinline__ void mbar_arrive(uint64_t* m) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+
+// pipeline state of one CTA: stage memory, the "full" mbarriers (completed by
+// the bulk copies' byte count), the "empty" mbarriers (one arrival per warp
+// once it has read the stage) and the number of stage fills consumed so far
+// (identical in every thread of the CTA)
 struct Pipe {
     unsigned char* stages;
-    uint64_t* mbar;
+    uint64_t* full;
+    uint64_t* empty;
     uint32_t consumed;
 };
 
 __device__ __forceinline__ void pipe_init(Pipe& pp, unsigned char* smem) {
     pp.stages = smem;
-    pp.mbar = reinterpret_cast<uint64_t*>(smem + kPipeBytes);
+    pp.full = reinterpret_cast<uint64_t*>(smem + kPipeBytes);
+    pp.empty = pp.full + kStages;
     pp.consumed = 0;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(pp.mbar + s, 1);
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(pp.full + s, 1);
+            mbar_init(pp.empty + s, kSimThreads / 32);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+}
+
+// error-free accumulation of an FP32 partial sum into an unevaluated pair
+// hi + lo (Knuth's TwoSum: the rounding error of hi + p is recovered exactly
+// and gathered in lo).  Six FP32 additions replace two FP64 ones: on this part
+// the FP64 pipe is ~64x narrower than FP32, and the fold runs once per 32
+// source columns for every row and instance.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
+    const float s = hi + p;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (p - bp);
+    hi = s;
+    lo += err;
+}
+
+// the R staged x values of one source column (stored contiguously, 16-byte
+// aligned when R * sizeof(X) is a multiple of 16)
+template <class X, int R>
+__device__ __forceinline__ void xload(const X* p, X x[R]) {
+    if constexpr (R * sizeof(X) % 16 == 0) {
+#pragma unroll
+        for (int k = 0; k < (int)(R * sizeof(X) / 16); ++k) {
+            const uint4 q = reinterpret_cast<const uint4*>(p)[k];
+            memcpy(reinterpret_cast<unsigned char*>(x) + 16 * k, &q, 16);
+        }
+    } else if constexpr (R * sizeof(X) == 8) {
+        const uint2 q = *reinterpret_cast<const uint2*>(p);
+        memcpy(x, &q, 8);
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) x[r] = p[r];
+    }
 }
 
 template <class M, int R>
@@ -285,6 +330,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     const unsigned char* Eb = reinterpret_cast<const unsigned char*>(p.E);
     const unsigned char* Kb = reinterpret_cast<const unsigned char*>(p.Kn);
     __shared__ long long s_tile;
+    __shared__ int s_abort;        // a bounded wait ran out in this tile
     for (;;) {
         // tiles are handed out by a global counter (reset once per step), so
         // CTAs that drew cheap tiles take more; results do not depend on the
@@ -297,93 +343,112 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
         const int64_t j0 = c * p.chunk_len;
         const int64_t L = min(N, j0 + p.chunk_len) - j0;
         const int64_t r0 = rb * rows_per_blk;
-        const int64_t rows_valid = min(rows_per_blk, N - r0);
-        // copy size: whole 16-byte granules; the padding up to ld is zero-filled
-        const uint32_t seg = (uint32_t)((rows_valid * EB + 15) / 16 * 16);
         const int nst = (int)((L + kColsPerStage - 1) / kColsPerStage);
         const uint32_t base = pp.consumed;
         auto fill = [&](int q) {   // thread 0 only
             const int slot = (int)((base + q) % kStages);
-            uint64_t* m = pp.mbar + slot;
+            uint64_t* m = pp.full + slot;
             const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
-            mbar_expect_tx(m, 2u * nc * seg);
+            // tile-contiguous layout: the nc columns of this row block are one
+            // run of nc * 4 KB in each matrix -> one bulk copy per matrix
+            const uint32_t bytes = (uint32_t)nc * kSegBytes;
+            mbar_expect_tx(m, 2u * bytes);
             unsigned char* st = pp.stages + (size_t)slot * kStageBytes;
-            for (int cc = 0; cc < nc; ++cc) {
-                const int64_t off = ((j0 + (int64_t)q * kColsPerStage + cc) * p.ld + r0) * EB;
-                bulk_g2s(st + (size_t)cc * kSegBytes, Eb + off, seg, m);
-                bulk_g2s(st + (size_t)(kColsPerStage + cc) * kSegBytes, Kb + off, seg, m);
-            }
+            const int64_t off = ((rb * N + j0 + (int64_t)q * kColsPerStage) * rows_per_blk) * EB;
+            bulk_g2s(st, Eb + off, bytes, m);
+            bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, Kb + off, bytes, m);
         };
-        __syncthreads();   // previous tile's stage reads and partial writes are done
+        // the counter read above was preceded by a barrier at which every
+        // thread had finished the previous tile's stages, x and partials
+        int issued = 0;                    // fills of this tile (thread 0)
         if (threadIdx.x == 0) {
+            s_abort = 0;
             fence_proxy_async();
-            for (int q = 0; q < min(kStages, nst); ++q) fill(q);
+            for (; issued < min(kStages, nst); ++issued) fill(issued);
         }
+        // x of this chunk, the R instances of one column side by side
         for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kSimThreads) {
             const int r = (int)(q / L);
             const int64_t j = q % L;
-            xs[r * p.chunk_len + j] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
+            xs[j * R + r] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
         }
         __syncthreads();
         const int64_t i0 = r0 + (int64_t)threadIdx.x * VEC;
-        double as[R][VEC], an[R][VEC];
+        // FP64 storage: fs/fn are the accumulators.  FP32 storage: fs/fn sum
+        // kFoldStages stages, then fold error-free into the pairs (h, l).
         X fs[R][VEC], fn[R][VEC];
+        float hs[R][VEC], ls[R][VEC], hn[R][VEC], ln[R][VEC];
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) { as[r][v] = 0.0; an[r][v] = 0.0; fs[r][v] = 0; fn[r][v] = 0; }
-        bool ok = true;
+            for (int v = 0; v < VEC; ++v) {
+                fs[r][v] = 0; fn[r][v] = 0;
+                hs[r][v] = 0.f; ls[r][v] = 0.f; hn[r][v] = 0.f; ln[r][v] = 0.f;
+            }
         for (int q = 0; q < nst; ++q) {
             const uint32_t n = base + q;
             const int slot = (int)(n % kStages);
-            if (!mbar_wait(pp.mbar + slot, (n / kStages) & 1u, kWaitLimitNs)) { ok = false; break; }
+            bool have = *(volatile int*)&s_abort == 0;
+            if (have && !mbar_wait(pp.full + slot, (n / kStages) & 1u, kWaitLimitNs)) {
+                *(volatile int*)&s_abort = 1;
+                have = false;
+            }
             const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
             const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * 16;
-            if (i0 < N) {
+            if (have && i0 < N) {
 #pragma unroll
                 for (int cc = 0; cc < kColsPerStage; ++cc) {
                     if (cc < nc) {
-                        X e[VEC], k[VEC];
+                        X e[VEC], k[VEC], x[R];
                         M::sload(st + (size_t)cc * kSegBytes, e);
                         M::sload(st + (size_t)(kColsPerStage + cc) * kSegBytes, k);
-                        const int64_t jj = (int64_t)q * kColsPerStage + cc;
+                        xload<X, R>(xs + ((int64_t)q * kColsPerStage + cc) * R, x);
 #pragma unroll
-                        for (int r = 0; r < R; ++r) {
-                            const X x = xs[r * p.chunk_len + jj];
+                        for (int r = 0; r < R; ++r)
 #pragma unroll
                             for (int v = 0; v < VEC; ++v) {
-                                fs[r][v] = fma(e[v], x, fs[r][v]);
-                                fn[r][v] = fma(k[v], x, fn[r][v]);
+                                fs[r][v] = fma(e[v], x[r], fs[r][v]);
+                                fn[r][v] = fma(k[v], x[r], fn[r][v]);
                             }
-                        }
                     }
                 }
-                if (sizeof(X) == 8 || (q & 7) == 7 || q == nst - 1) {
+                if constexpr (sizeof(X) == 4) {
+                    if ((q + 1) % kFoldStages == 0 || q == nst - 1) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r)
+                        for (int r = 0; r < R; ++r)
 #pragma unroll
-                        for (int v = 0; v < VEC; ++v) {
-                            as[r][v] += (double)fs[r][v];
-                            an[r][v] += (double)fn[r][v];
-                            fs[r][v] = 0;
-                            fn[r][v] = 0;
-                        }
+                            for (int v = 0; v < VEC; ++v) {
+                                two_sum_acc(hs[r][v], ls[r][v], (float)fs[r][v]);
+                                two_sum_acc(hn[r][v], ln[r][v], (float)fn[r][v]);
+                                fs[r][v] = 0;
+                                fn[r][v] = 0;
+                            }
+                    }
                 }
             }
-            __syncthreads();   // every thread is done with this slot
-            if (threadIdx.x == 0 && q + kStages < nst) {
-                fence_proxy_async();
-                fill(q + kStages);
+            // release the slot: one arrival per warp; thread 0 refills it once
+            // all warps have arrived, the others run ahead into filled stages
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) mbar_arrive(pp.empty + slot);
+            if (threadIdx.x == 0 && q + kStages < nst && *(volatile int*)&s_abort == 0) {
+                if (mbar_wait(pp.empty + slot, (n / kStages) & 1u, kWaitLimitNs)) {
+                    fence_proxy_async();
+                    fill(q + kStages);
+                    ++issued;
+                } else {
+                    *(volatile int*)&s_abort = 1;
+                }
             }
         }
         pp.consumed = base + nst;
-        if (!ok) {
-            // drain the fills this tile issued before giving up (bounded)
+        __syncthreads();
+        if (s_abort) {
+            // drain the copies still in flight: the last fill of each slot (bounded)
             if (threadIdx.x == 0) {
                 atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
-                for (int q = 0; q < nst; ++q) {
+                for (int q = max(0, issued - kStages); q < issued; ++q) {
                     const uint32_t n = base + q;
-                    mbar_wait(pp.mbar + (n % kStages), (n / kStages) & 1u, kWaitLimitNs);
+                    mbar_wait(pp.full + (n % kStages), (n / kStages) & 1u, kWaitLimitNs);
                 }
             }
             __syncthreads();
@@ -397,8 +462,13 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
                     const int64_t i = i0 + v;
                     if (i < N) {
                         const int64_t o = ((int64_t)c * R + r) * N + i;
-                        p.part_s[o] = as[r][v];
-                        p.part_n[o] = an[r][v];
+                        if constexpr (sizeof(X) == 8) {
+                            p.part_s[o] = fs[r][v];
+                            p.part_n[o] = fn[r][v];
+                        } else {
+                            p.part_s[o] = (double)hs[r][v] + (double)ls[r][v];
+                            p.part_n[o] = (double)hn[r][v] + (double)ln[r][v];
+                        }
                     }
                 }
         }
@@ -721,14 +791,18 @@ __global__ void k_chunk_reduce(SimParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// conversion kernels: source-major storage of ELSM and Kn in the chosen format
+// conversion kernel: ELSM = K_ij/K_ii and Kn in the chosen format, in the
+// tile-contiguous layout -- receivers in blocks of rpb rows (the operator
+// tile height), and within a block all source columns back to back:
+// entry (i, j) at ((i / rpb) * N + j) * rpb + i % rpb.  Rows past N are zero.
 __global__ void k_convert(const double* __restrict__ Ks, const double* __restrict__ Knm,
-                          int64_t N, int64_t ld_in, int layout, int64_t ld, int prec,
+                          int64_t N, int64_t ld_in, int layout, int64_t rpb, int prec,
                           void* E, void* Kn, double* kself) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // receiver
     const int64_t j = blockIdx.y;                                        // source (loops)
+    const int64_t nrows = (N + rpb - 1) / rpb * rpb;
     for (int64_t jj = j; jj < N; jj += gridDim.y) {
-        if (i >= ld) continue;
+        if (i >= nrows) continue;
         double e = 0.0, k = 0.0;
         if (i < N) {
             const int64_t in = layout == QDFN_LAYOUT_COL ? jj * ld_in + i : i * ld_in + jj;
@@ -738,7 +812,7 @@ __global__ void k_convert(const double* __restrict__ Ks, const double* __restric
             k = Knm[in];
             if (jj == 0) kself[i] = fabs(kii);
         }
-        const int64_t o = jj * ld + i;
+        const int64_t o = ((i / rpb) * N + jj) * rpb + i % rpb;
         if (prec == QDFN_FP64) {
             reinterpret_cast<double*>(E)[o] = e;
             reinterpret_cast<double*>(Kn)[o] = k;
@@ -1055,16 +1129,18 @@ int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t 
     c->E = c->Kn = nullptr;
     c->prec = precision;
     c->hmat = 0;
-    c->ld = (N + 31) / 32 * 32;
+    // ld holds the tile height (rows per block): 16 bytes per thread row group
     const size_t esz = precision == QDFN_FP64 ? 8 : 4;
-    const size_t mbytes = (size_t)N * c->ld * esz;
+    c->ld = (int64_t)kSimThreads * (int64_t)(16 / esz);
+    const int64_t nrows = (N + c->ld - 1) / c->ld * c->ld;
+    const size_t mbytes = (size_t)N * nrows * esz;
     unsigned char *dE = nullptr, *dK = nullptr;
     int rc = c->dalloc(&dE, mbytes);
     if (!rc) rc = c->dalloc(&dK, mbytes);
     if (rc) return rc;
     c->E = dE;
     c->Kn = dK;
-    dim3 grid((unsigned)((c->ld + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
+    dim3 grid((unsigned)((nrows + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
     k_convert<<<grid, 256, 0, st>>>(dKs, dKn, N, ld_in, layout, c->ld, precision, c->E, c->Kn, c->kself);
     QDFN_CUDA(cudaGetLastError());
     QDFN_CUDA(cudaStreamSynchronize(st));
