@@ -375,7 +375,13 @@ def run_ours(args):
                                    "operator": phases["ns_operator"] / 1e6 / args.steps,
                                    "friction_solves": phases["ns_solve"] / 1e6 / args.steps,
                                    "rotation": phases["ns_rotate"] / 1e6 / args.steps,
-                                   "solve_passes_per_step": phases["solve_passes"] / max(phases["steps"], 1)},
+                                   "solve_passes_per_step": phases["solve_passes"] / max(phases["steps"], 1),
+                                   "lowv_solves_per_step": phases["lowv_solves"] / max(phases["steps"], 1),
+                                   "lowv_iterations_per_solve":
+                                       phases["lowv_iterations"] / max(phases["lowv_solves"], 1),
+                                   "highv_solves_per_step": phases["highv_solves"] / max(phases["steps"], 1),
+                                   "highv_iterations_per_solve":
+                                       phases["highv_iterations"] / max(phases["highv_solves"], 1)},
             "clocks": clk,
         }
         print(json.dumps(line))

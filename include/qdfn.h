@@ -179,7 +179,10 @@ int qdfn_sync(qdfn_ctx* ctx);
 int qdfn_kernels_per_run(const qdfn_ctx* ctx);
 /* Cumulative device counters of the context's runs (first n of): ns spent in
  * [0] time-step control, [1] elastic operator, [2] friction solves and retries,
- * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps. */
+ * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps;
+ * [6] low-velocity patch solves, [7] their secant iterations, [8] high-velocity
+ * patch solves, [9] their secant iterations (summed over patches, instances
+ * (padding instances included) and solve passes). */
 int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */

@@ -36,6 +36,7 @@ constexpr int kSimThreads = 256;
 constexpr int kMaxInst = 4;
 constexpr int kRedSlots = 8;                // doubles per (CTA, instance) partial
 constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
+constexpr int kCounters = 10;               // qdfn_get_counters slots
 
 // ---------------------------------------------------------------------------
 // matrix element formats: each thread owns VEC consecutive receiver rows, one
@@ -318,6 +319,57 @@ __device__ __forceinline__ void xload(const X* p, X x[R]) {
     }
 }
 
+// Sum of the column-chunk partials of row (instance r, receiver i), in chunk
+// order (deterministic).  FP64 storage: the partials are doubles, summed in
+// FP64.  FP32/BF16 storage (kPairs): each partial is the tile's (hi, lo) FP32
+// pair; the hi parts are gathered error-free with TwoSum and the lo parts
+// added, all on the FP32 pipe, and the pair becomes a double once per row.
+// Loads are issued eight chunks at a time so they overlap.
+template <bool kPairs>
+__device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t i, double& ss,
+                                             double& sn) {
+    const int64_t cs = (int64_t)p.R * p.N;
+    const int64_t base = (int64_t)r * p.N + i;
+    if constexpr (kPairs) {
+        const float2* ps = reinterpret_cast<const float2*>(p.part_s) + base;
+        const float2* pn = reinterpret_cast<const float2*>(p.part_n) + base;
+        float hs = 0.f, ls = 0.f, hn = 0.f, ln = 0.f;
+        int c = 0;
+        for (; c + 8 <= p.nchunk; c += 8) {
+            float2 ts[8], tn[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                two_sum_acc(hs, ls, ts[k].x); ls += ts[k].y;
+                two_sum_acc(hn, ln, tn[k].x); ln += tn[k].y;
+            }
+        }
+        for (; c < p.nchunk; ++c) {
+            const float2 a = __ldcg(ps + c * cs), b = __ldcg(pn + c * cs);
+            two_sum_acc(hs, ls, a.x); ls += a.y;
+            two_sum_acc(hn, ln, b.x); ln += b.y;
+        }
+        ss = (double)hs + (double)ls;
+        sn = (double)hn + (double)ln;
+    } else {
+        const double* ps = p.part_s + base;
+        const double* pn = p.part_n + base;
+        double as = 0, an = 0;
+        int c = 0;
+        for (; c + 8 <= p.nchunk; c += 8) {
+            double ts[8], tn[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) { as += ts[k]; an += tn[k]; }
+        }
+        for (; c < p.nchunk; ++c) { as += __ldcg(ps + c * cs); an += __ldcg(pn + c * cs); }
+        ss = as;
+        sn = an;
+    }
+}
+
 template <class M, int R>
 __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     using X = typename M::X;
@@ -465,9 +517,9 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
                         if constexpr (sizeof(X) == 8) {
                             p.part_s[o] = fs[r][v];
                             p.part_n[o] = fn[r][v];
-                        } else {
-                            p.part_s[o] = (double)hs[r][v] + (double)ls[r][v];
-                            p.part_n[o] = (double)hn[r][v] + (double)ln[r][v];
+                        } else {   // the pair itself: no FP64 work in this phase
+                            reinterpret_cast<float2*>(p.part_s)[o] = make_float2(hs[r][v], ls[r][v]);
+                            reinterpret_cast<float2*>(p.part_n)[o] = make_float2(hn[r][v], ln[r][v]);
                         }
                     }
                 }
@@ -495,6 +547,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     // phase timers of CTA 0 (all CTAs leave each barrier together)
     uint64_t tp[4] = {0, 0, 0, 0}, tmark = globaltimer_ns();
     unsigned long long n_iter = 0, n_steps = 0;
+    unsigned long long n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations
     auto lap = [&](int k) { const uint64_t t = globaltimer_ns(); tp[k] += t - tmark; tmark = t; };
     const int64_t N = p.N, Ns = p.N - p.Nload;
     const int64_t nthreads = (int64_t)gridDim.x * kSimThreads;
@@ -591,7 +644,12 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             double v[kMaxInst][4];
             for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
             const int first = (s_iter == 0);
-            for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+            // every CTA takes an equal contiguous range of (instance, patch)
+            // items: the solves are FP64-pipe bound, so the per-SM item count
+            // sets the phase time
+            const int64_t per_cta = ((int64_t)R * N + gridDim.x - 1) / gridDim.x;
+            const int64_t q_end = min((int64_t)R * N, (int64_t)blockIdx.x * per_cta + per_cta);
+            for (int64_t q = (int64_t)blockIdx.x * per_cta + threadIdx.x; q < q_end; q += kSimThreads) {
                 const int r = (int)(q / N);
                 if (s_done[r]) continue;
                 const int64_t i = q - (int64_t)r * N;
@@ -602,11 +660,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         p.tld[q] = (-ss) / -p.kself[i];
                         p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
                     } else {
-                        double ss = 0, sn = 0;
-                        for (int c = 0; c < p.nchunk; ++c) {
-                            ss += __ldcg(p.part_s + ((int64_t)c * R + r) * N + i);
-                            sn += __ldcg(p.part_n + ((int64_t)c * R + r) * N + i);
-                        }
+                        double ss, sn;
+                        sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
                         p.tld[q] = -ss;   // ELSM * (0 - DispOld)
                         p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
                     }
@@ -632,6 +687,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         : sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
                     p.Vn[q] = o.V; p.fn[q] = o.Friction; p.Dn[q] = o.Disp; p.thn[q] = o.Theta;
                     p.sn[q] = sig; p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
+                    if (p.sw[q] == 1) { ++n_hi; it_hi += o.Iterations; }
+                    else { ++n_lo; it_lo += o.Iterations; }
                     if (err) v[r][3] = fmin(v[r][3], (double)err);
                     v[r][0] = fmin(v[r][0], (double)o.Flag);
                     v[r][1] = fmin(v[r][1], o.Dt);
@@ -734,6 +791,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         atomicAdd(p.prof + 4, n_iter);
         atomicAdd(p.prof + 5, n_steps);
     }
+    if (p.prof) {   // solver work of every thread, one atomic per warp and counter
+        unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            for (int o = 16; o > 0; o >>= 1) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+            if ((threadIdx.x & 31) == 0 && w[k]) atomicAdd(p.prof + 6 + k, w[k]);
+        }
+    }
     if (blockIdx.x == 0 && threadIdx.x < R) {
         const int r = threadIdx.x;
         p.T[r] = s_T[r];
@@ -776,16 +841,14 @@ __global__ void k_hmat_rows(SimParams p) {
     p.knd[q] = hmat::row_sum<R>(p.h, 1, p.N, i, r);
 }
 
+template <bool kPairs>
 __global__ void k_chunk_reduce(SimParams p) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (int64_t)p.R * p.N) return;
     const int r = (int)(q / p.N);
     const int64_t i = q - (int64_t)r * p.N;
-    double ss = 0, sn = 0;
-    for (int c = 0; c < p.nchunk; ++c) {
-        ss += p.part_s[((int64_t)c * p.R + r) * p.N + i];
-        sn += p.part_n[((int64_t)c * p.R + r) * p.N + i];
-    }
+    double ss, sn;
+    sum_partials<kPairs>(p, r, i, ss, sn);
     p.tld[q] = -ss;
     p.knd[q] = sn;
 }
@@ -1061,7 +1124,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
-    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, 8); A(tile_ctr, 1);
+    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, kCounters); A(tile_ctr, 1);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
@@ -1266,9 +1329,9 @@ extern "C" int qdfn_kernels_per_run(const qdfn_ctx* c) { return c ? 1 : 0; }
 
 extern "C" int qdfn_get_counters(const qdfn_ctx* c, int64_t* out, int n) {
     if (!c || !out || n < 0) return fail(QDFN_ERR_INVALID, "null argument");
-    unsigned long long v[8];
+    unsigned long long v[kCounters];
     QDFN_CUDA(cudaMemcpy(v, c->prof, sizeof(v), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < n && k < 8; ++k) out[k] = (int64_t)v[k];
+    for (int k = 0; k < n && k < kCounters; ++k) out[k] = (int64_t)v[k];
     return QDFN_OK;
 }
 
@@ -1351,7 +1414,8 @@ extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, do
         QDFN_CUDA(cudaMemset(c->tile_ctr, 0, sizeof(unsigned long long)));
         apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
         QDFN_CUDA(cudaGetLastError());
-        k_chunk_reduce<<<(unsigned)((tot + 255) / 256), 256>>>(p);
+        if (c->prec == QDFN_FP64) k_chunk_reduce<false><<<(unsigned)((tot + 255) / 256), 256>>>(p);
+        else k_chunk_reduce<true><<<(unsigned)((tot + 255) / 256), 256>>>(p);
         QDFN_CUDA(cudaGetLastError());
     }
     QDFN_CUDA(cudaDeviceSynchronize());

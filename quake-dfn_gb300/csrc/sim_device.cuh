@@ -30,6 +30,7 @@ struct PatchIn {
 struct PatchOut {
     double V, Friction, Disp, Theta, Dt;
     int Instab, Flag;
+    int Iterations;      // secant iterations taken (diagnostics)
 };
 
 __device__ __forceinline__ double jlog(double x, int& err) {
@@ -48,22 +49,71 @@ __device__ __forceinline__ bool alpha_term_zero(double alpha, double Dt, double 
            isfinite(sig_old) && isfinite(b) && b != 0.0;
 }
 
-__device__ __forceinline__ double evolution(double ThetaOld, double Dt, double V, double Dc,
+// Division by a divisor that stays fixed for a whole solve.  With y = 1/d
+// correctly rounded (one IEEE division per solve), q0 = x*y is within an ulp
+// of x/d, the remainder r = x - q0*d is exact in one FMA, and q0 + r*y rounds
+// to x/d (Markstein's correction step: P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990).  Three FP64 operations instead of the eight of a full division.  The
+// sum is formed as -fma(-r, y, -q0) so that x = -0 keeps its sign.  Operands
+// whose magnitudes leave [2^-895, 2^896] (or a divisor that is zero, infinite
+// or NaN) take the full division, so no step can overflow or underflow.
+struct Recip {
+    double d, y;
+    bool ok;
+};
+__device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >> 20) & 0x7ff; }
+__device__ __forceinline__ bool in_safe_range(int e) { return (unsigned)(e - 128) <= 1791u; }
+__device__ __forceinline__ Recip recip(double d) {
+    Recip r;
+    r.d = d;
+    r.y = 1.0 / d;
+    r.ok = in_safe_range(exp_field(d));
+    return r;
+}
+__device__ __noinline__ double full_div(double x, double d) { return x / d; }
+__device__ __forceinline__ double div_by(double x, const Recip& R) {
+    const double q0 = x * R.y;
+    const double r = fma(-q0, R.d, x);
+    const double q = -fma(-r, R.y, -q0);
+    const bool zero = (__double_as_longlong(x) << 1) == 0;
+    const bool fast = R.ok && (zero || (in_safe_range(exp_field(x)) && in_safe_range(exp_field(q0))));
+    if (fast) return q;
+    return full_div(x, R.d);   // out of line: never evaluated speculatively
+}
+
+// The alpha terms as written in the reference.  Out of line so that the
+// compiler cannot evaluate them speculatively next to the (usual) skip path.
+__device__ __noinline__ double alpha_term_fast(double alpha, double sig, double sig_old, double Dt,
+                                               double b) {
+    return alpha * (sig - sig_old) / Dt / b / sig;
+}
+__device__ __noinline__ double alpha_term_slow(double alpha, double sig, double sig_old, double Dt,
+                                               double b) {
+    return alpha * Dt * (sig - sig_old) / Dt / b / sig;
+}
+
+// `skip` = alpha_term_zero(alpha, Dt, sig, sig_old, b), evaluated once per
+// solve by the caller: its operands do not change between the evolution calls
+// of one solve (Dt is only halved on the way out of the secant loop).
+__device__ __forceinline__ double evolution(double ThetaOld, double Dt, double V, const Recip& Rdc,
                                             double alpha, double sig, double sig_old, double b,
-                                            int fast, int dr, int& err) {
+                                            int fast, int dr, bool skip, int& err) {
     if (dr == 1) {
-        const bool skip = alpha_term_zero(alpha, Dt, sig, sig_old, b);
         if (fast) {
-            const double vd = V / Dc;
-            const double Const_T = (skip && vd != 0.0) ? vd : vd + alpha * (sig - sig_old) / Dt / b / sig;
+            const double vd = div_by(V, Rdc);
+            double Const_T = vd;
+            if (!(skip && vd != 0.0)) Const_T = vd + alpha_term_fast(alpha, sig, sig_old, Dt, b);
             // (-V)/Dc == -(V/Dc) exactly, so the quotient is reused
             return (ThetaOld - 1 / Const_T) * exp(-vd * Dt) + 1 / Const_T;
         }
-        const double den0 = 1 + Dt * V / Dc;
-        const double den = (skip && den0 != 0.0) ? den0 : den0 + alpha * Dt * (sig - sig_old) / Dt / b / sig;
+        const double den0 = 1 + div_by(Dt * V, Rdc);
+        double den = den0;
+        if (!(skip && den0 != 0.0)) den = den0 + alpha_term_slow(alpha, sig, sig_old, Dt, b);
         return (ThetaOld + Dt) / den;
     }
-    return ThetaOld - V * ThetaOld / Dc * jlog(V * ThetaOld / Dc, err) * Dt;
+    const double w = div_by(V * ThetaOld, Rdc);
+    return ThetaOld - w * jlog(w, err) * Dt;
 }
 
 // Semi-analytic harmonic-oscillator update with a secant iteration on V.
@@ -74,29 +124,34 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
     const double DV = p.VOld / 100;
     double V = p.VOld / 1e10, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
     if (V < 0) V = 1e-100;
+    const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
+    // the reference evaluates cos/sin(Omega Dt) in every iteration; Dt is
+    // constant for every iteration that reaches them, so once is the same
+    const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
+    // divisors fixed for the solve (Dt only changes on the way out of the loop)
+    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt);
 #define QDFN_RESET() do { V = p.VOld; Theta = p.ThetaOld; Friction = p.FrictionOld; Disp = p.DispOld; } while (0)
     while (maxDiff > crit) {
         Iteration++;
         if (Iteration > kHighVIterCap) { err = QDFN_ERR_NO_CONVERGE; break; }
         const double VTest = V;
-        Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, err);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
         if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-        const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
-        double Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(Theta * kV0 / p.Dc, err) +
+        double Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err) +
                     eta / p.sigma * V - p.dtau / p.sigma;
         double F = p.TLD + (p.tau0 - Fr * p.sigma) / p.K_Self;
         Disp = (p.DispOld - F) * cO + (p.VOld / p.Omega) * sO + F;
-        V = (Disp - p.DispOld) / Dt * 2 - p.VOld;
+        V = div_by(Disp - p.DispOld, Rdt) * 2 - p.VOld;
         const double FOriginal = VTest - V;
         V = VTest + DV;
         const double VTest2 = V;
-        Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, err);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
         if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-        Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(Theta * kV0 / p.Dc, err) +
+        Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err) +
              eta / p.sigma * V - p.dtau / p.sigma;
         F = p.TLD + (p.tau0 - Fr * p.sigma) / p.K_Self;
         Disp = (p.DispOld - F) * cO + (p.VOld / p.Omega) * sO + F;
-        V = (Disp - p.DispOld) / Dt * 2 - p.VOld;
+        V = div_by(Disp - p.DispOld, Rdt) * 2 - p.VOld;
         const double FUpdated = VTest2 - V;
         V = VTest - FOriginal * DV / (FUpdated - FOriginal);
         if (V < 0 || isnan(V)) {
@@ -107,9 +162,9 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
             else { Dt = Dt / 2; Instab = 4; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
         } else {
             Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
-            Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, err);
+            Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
             if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-            Friction = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(Theta * kV0 / p.Dc, err);
+            Friction = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err);
             maxDiff = fabs(VTest / V - 1);
             Instab = 0;
         }
@@ -121,7 +176,7 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
     }
     PatchOut o;
     o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
-    o.Instab = Instab; o.Flag = FLAG;
+    o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
     return o;
 }
 
@@ -133,7 +188,12 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
     double maxDiff = 10, crit = kConv;
     double V = p.VOld, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
     const double inv_sig = 1 / p.sigma;
-#define QDFN_FAIL_A()                                                      \
+    const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
+    // divisors fixed for the solve (Dt only changes on the way out of the loop);
+    // 1e-10 is the correctly rounded reciprocal of 1e10 (both are 10^-10 rounded)
+    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt), Ra = recip(p.a);
+    const Recip R1e10 = {1e10, 1e-10, true};
+#define QDFN_FAIL_A()                                                    \
     do {                                                                   \
         if (Dt < SwitchV) { Instab = 3; QDFN_RESET(); FLAG = 0; }          \
         else if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }                  \
@@ -144,29 +204,29 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
     while (maxDiff > crit) {
         Iteration++;
         const double VTest = V;
-        const double DV = VTest / 1e10;
-        double Accel = (V - p.VOld) / Dt;
-        Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, err);
+        const double DV = div_by(VTest, R1e10);
+        double Accel = div_by(V - p.VOld, Rdt);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
         if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
         Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
         Friction = QDFN_FRICTION(V, Disp, Accel);
-        double Vel = kV0 * exp((Friction - p.Friction0 - p.b * jlog(kV0 * Theta / p.Dc, err)) / p.a);
+        double Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
         const double FV = VTest - Vel;
         V = V + DV;
         const double VTest2 = V;
-        Accel = (V - p.VOld) / Dt;
-        Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, err);
+        Accel = div_by(V - p.VOld, Rdt);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
         if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
         Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
         Friction = QDFN_FRICTION(V, Disp, Accel);
-        Vel = kV0 * exp((Friction - p.Friction0 - p.b * jlog(kV0 * Theta / p.Dc, err)) / p.a);
+        Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
         const double FV_DeV = VTest2 - Vel;
         V = VTest - FV * DV / (FV_DeV - FV);
         if (dr != 1 && V < 0)
             V = exp(jlog(VTest, err) - FV * jlog(VTest2 / VTest, err) / (FV_DeV - FV));
-        Accel = (V - p.VOld) / Dt;
+        Accel = div_by(V - p.VOld, Rdt);
         Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
-        Theta = evolution(p.ThetaOld, Dt, V, p.Dc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, err);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
         if (Theta < 0) { QDFN_FAIL_A(); break; }
         if (isnan(Theta)) {
             if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }
@@ -193,7 +253,7 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
 #undef QDFN_RESET
     PatchOut o;
     o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
-    o.Instab = Instab; o.Flag = FLAG;
+    o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
     return o;
 }
 
