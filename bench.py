@@ -374,6 +374,8 @@ def run_ours(args):
             "phases_ms_per_step": {"time_control": phases["ns_control"] / 1e6 / args.steps,
                                    "operator": phases["ns_operator"] / 1e6 / args.steps,
                                    "friction_solves": phases["ns_solve"] / 1e6 / args.steps,
+                                   "friction_solves_block0_own": phases["ns_solve_own"] / 1e6 / args.steps,
+                                   "friction_solves_block0_wait": phases["ns_solve_wait"] / 1e6 / args.steps,
                                    "rotation": phases["ns_rotate"] / 1e6 / args.steps,
                                    "solve_passes_per_step": phases["solve_passes"] / max(phases["steps"], 1),
                                    "lowv_solves_per_step": phases["lowv_solves"] / max(phases["steps"], 1),

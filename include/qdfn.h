@@ -182,7 +182,9 @@ int qdfn_kernels_per_run(const qdfn_ctx* ctx);
  * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps;
  * [6] low-velocity patch solves, [7] their secant iterations, [8] high-velocity
  * patch solves, [9] their secant iterations (summed over patches, instances
- * (padding instances included) and solve passes). */
+ * (padding instances included) and solve passes); [10] ns of [2] that the
+ * first block spent on its own solves and block reduction, [11] ns of [2] it
+ * waited at the grid barrier after them. */
 int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */

@@ -42,7 +42,7 @@ struct Ops {
     const int64_t* rowslot;  // slot indices
 };
 
-constexpr int kTileRows = 256;
+constexpr int kTileRows = 512;     // one receiver row per thread of a 512-thread block
 constexpr int kChunk = 1024;
 constexpr int kMaxRank = 128;
 

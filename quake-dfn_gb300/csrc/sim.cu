@@ -32,40 +32,38 @@
 namespace qdfn {
 namespace {
 
-constexpr int kSimThreads = 256;
+constexpr int kSimThreads = 512;
+constexpr int kGranule = 8;                 // operator bytes per thread and source column
 constexpr int kMaxInst = 4;
 constexpr int kRedSlots = 8;                // doubles per (CTA, instance) partial
 constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
-constexpr int kCounters = 10;               // qdfn_get_counters slots
+constexpr int kCounters = 12;               // qdfn_get_counters slots
 
 // ---------------------------------------------------------------------------
 // matrix element formats: each thread owns VEC consecutive receiver rows, one
-// 16-byte granule per source column (sload decodes it from shared memory).
+// kGranule-byte granule per source column (sload decodes it from shared memory).
 struct FmtF64 {
-    static constexpr int VEC = 2;
+    static constexpr int VEC = 1;
     using X = double;  // staged x type
-    __device__ __forceinline__ static void sload(const unsigned char* p, double v[2]) {
-        const double2 q = *reinterpret_cast<const double2*>(p);
-        v[0] = q.x; v[1] = q.y;
+    __device__ __forceinline__ static void sload(const unsigned char* p, double v[1]) {
+        v[0] = *reinterpret_cast<const double*>(p);
     }
 };
 struct FmtF32 {
-    static constexpr int VEC = 4;
+    static constexpr int VEC = 2;
     using X = float;
-    __device__ __forceinline__ static void sload(const unsigned char* p, float v[4]) {
-        const float4 q = *reinterpret_cast<const float4*>(p);
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    __device__ __forceinline__ static void sload(const unsigned char* p, float v[2]) {
+        const float2 q = *reinterpret_cast<const float2*>(p);
+        v[0] = q.x; v[1] = q.y;
     }
 };
 struct FmtBF16x2 {  // each 32-bit word: hi bf16 in the upper half, lo bf16 in the lower half
-    static constexpr int VEC = 4;
+    static constexpr int VEC = 2;
     using X = float;
-    __device__ __forceinline__ static void sload(const unsigned char* p, float v[4]) {
-        const uint4 q = *reinterpret_cast<const uint4*>(p);
-        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            v[k] = __uint_as_float(w[k] & 0xFFFF0000u) + __uint_as_float(w[k] << 16);
+    __device__ __forceinline__ static void sload(const unsigned char* p, float v[2]) {
+        const uint2 q = *reinterpret_cast<const uint2*>(p);
+        v[0] = __uint_as_float(q.x & 0xFFFF0000u) + __uint_as_float(q.x << 16);
+        v[1] = __uint_as_float(q.y & 0xFFFF0000u) + __uint_as_float(q.y << 16);
     }
 };
 
@@ -137,20 +135,35 @@ __device__ bool grid_barrier(const SimParams& p, uint64_t deadline_ns) {
     return s_ok != 0;
 }
 
-// block-wide reduction of R*K doubles with op (0 = max, 1 = min, 2 = sum)
+// Order-preserving map of doubles to unsigned 64-bit keys (sign bit flipped
+// for x >= 0, all bits inverted for x < 0): min/max of keys is min/max of the
+// values, on the integer pipe.  The FP64 pipe of this part is ~64x narrower
+// than FP32, and these reductions run twice per step.  The reduced fields
+// never hold NaN (a NaN velocity is carried by its own flag field), so the
+// result equals fmin/fmax; the order of +0/-0 is -0 < +0.
+__device__ __forceinline__ unsigned long long ord_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b ^ ((unsigned long long)((long long)b >> 63) | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_val(unsigned long long k) {
+    const unsigned long long b = (k & 0x8000000000000000ull) ? (k ^ 0x8000000000000000ull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ unsigned long long key_op(int op, unsigned long long a, unsigned long long b) {
+    return op == 0 ? (a > b ? a : b) : (a < b ? a : b);
+}
+
+// block-wide reduction of R*K doubles with op (0 = max, 1 = min)
 template <int K>
 __device__ void block_reduce(double (&v)[kMaxInst][K], const int (&ops)[K], int R) {
-    __shared__ double s_buf[kSimThreads / 32][kMaxInst][K];
+    __shared__ unsigned long long s_buf[kSimThreads / 32][kMaxInst][K];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            double x = v[r][k];
+            unsigned long long x = ord_key(v[r][k]);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double y = __shfl_xor_sync(0xffffffffu, x, o);
-                x = ops[k] == 0 ? fmax(x, y) : ops[k] == 1 ? fmin(x, y) : x + y;
-            }
+            for (int o = 16; o > 0; o >>= 1) x = key_op(ops[k], x, __shfl_xor_sync(0xffffffffu, x, o));
             if (lane == 0) s_buf[wid][r][k] = x;
         }
     __syncthreads();
@@ -158,12 +171,9 @@ __device__ void block_reduce(double (&v)[kMaxInst][K], const int (&ops)[K], int 
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                double x = s_buf[0][r][k];
-                for (int w = 1; w < kSimThreads / 32; ++w) {
-                    const double y = s_buf[w][r][k];
-                    x = ops[k] == 0 ? fmax(x, y) : ops[k] == 1 ? fmin(x, y) : x + y;
-                }
-                v[r][k] = x;
+                unsigned long long x = s_buf[0][r][k];
+                for (int w = 1; w < kSimThreads / 32; ++w) x = key_op(ops[k], x, s_buf[w][r][k]);
+                v[r][k] = ord_val(x);
             }
     }
     __syncthreads();
@@ -177,30 +187,27 @@ template <int K>
 __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, int R, int r,
                                             const int (&ops)[K], double (&out)[K]) {
     const int lane = threadIdx.x & 31;
+    unsigned long long acc[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) out[k] = ops[k] == 0 ? -INFINITY : INFINITY;
+    for (int k = 0; k < K; ++k) acc[k] = ord_key(ops[k] == 0 ? -INFINITY : INFINITY);
     for (int b = lane; b < nblk; b += 32) {
         const double* s = slots_base + ((int64_t)b * R + r) * kRedSlots;
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const double x = __ldcg(s + k);
-            out[k] = ops[k] == 0 ? fmax(out[k], x) : fmin(out[k], x);
-        }
+        for (int k = 0; k < K; ++k) acc[k] = key_op(ops[k], acc[k], ord_key(__ldcg(s + k)));
     }
 #pragma unroll
-    for (int k = 0; k < K; ++k)
+    for (int k = 0; k < K; ++k) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double y = __shfl_xor_sync(0xffffffffu, out[k], o);
-            out[k] = ops[k] == 0 ? fmax(out[k], y) : fmin(out[k], y);
-        }
+        for (int o = 16; o > 0; o >>= 1) acc[k] = key_op(ops[k], acc[k], __shfl_xor_sync(0xffffffffu, acc[k], o));
+        out[k] = ord_val(acc[k]);
+    }
 }
 
 // ---------------------------------------------------------------------------
 // P2: dense elastic operator.
 //
 // Storage is tile-contiguous: receivers in row blocks of kSimThreads*VEC (one
-// 16-byte granule per thread and source column, 4 KB per column), and within a
+// 8-byte granule per thread and source column, 4 KB per column), and within a
 // row block the source columns back to back (see k_convert).  A tile is (row
 // block, chunk of source columns); tiles are handed out by a global counter.
 // Both matrices stream through a kStages-deep ring of 64 KB shared-memory
@@ -208,12 +215,13 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 // (cp.async.bulk ... mbarrier::complete_tx) issued by one thread, so the bytes
 // in flight do not depend on the register-limited warp count of the
 // persistent kernel.  x = D (all R instances) is staged per tile.  FP32/BF16
-// products are summed in FP32 over 32 columns and folded into FP64
-// accumulators; FP64 storage accumulates in FP64.
+// products are summed in FP32 over 32 columns and folded error-free into
+// (hi, lo) FP32 pairs; FP64 storage accumulates in FP64.
+static_assert(hmat::kTileRows == kSimThreads, "H-matrix row tiles are one row per thread");
 constexpr int kStages = 3;
 constexpr int kColsPerStage = 8;
 constexpr int kFoldStages = 32 / kColsPerStage;                 // FP32 sums span 32 columns
-constexpr int kSegBytes = kSimThreads * 16;                     // one column of a row block
+constexpr int kSegBytes = kSimThreads * kGranule;               // one column of a row block, 4 KB
 constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn, 64 KB
 constexpr int kPipeBytes = kStages * kStageBytes;               // 192 KB
 constexpr int kMbarBytes = 128;
@@ -229,11 +237,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
+// L2 policy for data read once per step (the operator stream): evict first,
+// so that what the step re-reads (chunk partials, state) stays in L2
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m,
+                                         uint64_t pol) {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(m))
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(m)), "l"(pol)
         : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
@@ -374,7 +390,7 @@ template <class M, int R>
 __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
-    constexpr int EB = 16 / VEC;   // bytes per stored entry
+    constexpr int EB = kGranule / VEC;   // bytes per stored entry
     constexpr int64_t rows_per_blk = (int64_t)kSimThreads * VEC;
     const int64_t N = p.N;
     const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
@@ -383,6 +399,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     const unsigned char* Kb = reinterpret_cast<const unsigned char*>(p.Kn);
     __shared__ long long s_tile;
     __shared__ int s_abort;        // a bounded wait ran out in this tile
+    const uint64_t pol = l2_evict_first_policy();
     for (;;) {
         // tiles are handed out by a global counter (reset once per step), so
         // CTAs that drew cheap tiles take more; results do not depend on the
@@ -407,8 +424,8 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
             mbar_expect_tx(m, 2u * bytes);
             unsigned char* st = pp.stages + (size_t)slot * kStageBytes;
             const int64_t off = ((rb * N + j0 + (int64_t)q * kColsPerStage) * rows_per_blk) * EB;
-            bulk_g2s(st, Eb + off, bytes, m);
-            bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, Kb + off, bytes, m);
+            bulk_g2s(st, Eb + off, bytes, m, pol);
+            bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, Kb + off, bytes, m, pol);
         };
         // the counter read above was preceded by a barrier at which every
         // thread had finished the previous tile's stages, x and partials
@@ -446,7 +463,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
                 have = false;
             }
             const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
-            const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * 16;
+            const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * kGranule;
             if (have && i0 < N) {
 #pragma unroll
                 for (int cc = 0; cc < kColsPerStage; ++cc) {
@@ -546,6 +563,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     const uint64_t deadline = globaltimer_ns() + p.budget_ns;
     // phase timers of CTA 0 (all CTAs leave each barrier together)
     uint64_t tp[4] = {0, 0, 0, 0}, tmark = globaltimer_ns();
+    uint64_t tq[2] = {0, 0};   // P3 split: own items + block reduce / grid barrier wait
     unsigned long long n_iter = 0, n_steps = 0;
     unsigned long long n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations
     auto lap = [&](int k) { const uint64_t t = globaltimer_ns(); tp[k] += t - tmark; tmark = t; };
@@ -640,6 +658,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         // ---------------------------------------------------------- P3
         if (threadIdx.x == 0) s_iter = 0;
         __syncthreads();
+        uint64_t tmark_p3 = globaltimer_ns();
         for (;;) {
             double v[kMaxInst][4];
             for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
@@ -712,7 +731,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     double* s = red_slot(phase, blockIdx.x, r);
                     s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
                 }
+            const uint64_t t_items = globaltimer_ns();
             if (!grid_barrier(p, deadline)) return;
+            {   // CTA 0: own solves + block reduction, then the wait for the grid
+                const uint64_t t = globaltimer_ns();
+                tq[0] += t_items - tmark_p3;
+                tq[1] += t - t_items;
+                tmark_p3 = t;
+            }
             if ((threadIdx.x >> 5) < R) {
                 const int r = threadIdx.x >> 5;
                 if (!s_done[r]) {
@@ -790,6 +816,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         for (int k = 0; k < 4; ++k) atomicAdd(p.prof + k, (unsigned long long)tp[k]);
         atomicAdd(p.prof + 4, n_iter);
         atomicAdd(p.prof + 5, n_steps);
+        atomicAdd(p.prof + 10, (unsigned long long)tq[0]);
+        atomicAdd(p.prof + 11, (unsigned long long)tq[1]);
     }
     if (p.prof) {   // solver work of every thread, one atomic per warp and counter
         unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};
@@ -1037,7 +1065,7 @@ void hmat_apply_kernels(int R, ApplyKernel* a, ApplyKernel* b, ApplyKernel* rows
 
 int configure_launch(qdfn_ctx* c) {
     const int Rk = kernel_R(c->R);
-    const int vec = c->prec == QDFN_FP64 ? 2 : 4;
+    const int vec = c->prec == QDFN_FP64 ? 1 : 2;
     const size_t xsz = c->prec == QDFN_FP64 ? 8 : 4;
     const int sms = num_sms();
     if (sms <= 0) return fail(QDFN_ERR_CUDA, "no CUDA device");
@@ -1194,7 +1222,7 @@ int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t 
     c->hmat = 0;
     // ld holds the tile height (rows per block): 16 bytes per thread row group
     const size_t esz = precision == QDFN_FP64 ? 8 : 4;
-    c->ld = (int64_t)kSimThreads * (int64_t)(16 / esz);
+    c->ld = (int64_t)kSimThreads * (int64_t)(kGranule / esz);
     const int64_t nrows = (N + c->ld - 1) / c->ld * c->ld;
     const size_t mbytes = (size_t)N * nrows * esz;
     unsigned char *dE = nullptr, *dK = nullptr;
