@@ -372,10 +372,15 @@ def run_ours(args):
             "accuracy_horizon": horizon,
             "assembly": {"pairs": N * N, "ms": asm_ms, "pairs_per_s": N * N / (asm_ms / 1e3)},
             "phases_ms_per_step": {"time_control": phases["ns_control"] / 1e6 / args.steps,
-                                   "operator": phases["ns_operator"] / 1e6 / args.steps,
-                                   "friction_solves": phases["ns_solve"] / 1e6 / args.steps,
-                                   "friction_solves_block0_own": phases["ns_solve_own"] / 1e6 / args.steps,
-                                   "friction_solves_block0_wait": phases["ns_solve_wait"] / 1e6 / args.steps,
+                                   "operator_with_overlapped_solves": phases["ns_operator"] / 1e6 / args.steps,
+                                   "block0_operator_warps": phases["ns_operator_warps"] / 1e6 / args.steps,
+                                   "block0_solver_warps": phases["ns_solver_warps"] / 1e6 / args.steps,
+                                   "slowest_block_operator_warps":
+                                       phases["ns_operator_warps_slowest"] / 1e6 / args.steps,
+                                   "slowest_block_solver_warps": phases["ns_solver_warps_slowest"] / 1e6 / args.steps,
+                                   "solve_reduce_and_retries": phases["ns_solve"] / 1e6 / args.steps,
+                                   "block0_retry_solves": phases["ns_solve_own"] / 1e6 / args.steps,
+                                   "block0_barrier_wait": phases["ns_solve_wait"] / 1e6 / args.steps,
                                    "rotation": phases["ns_rotate"] / 1e6 / args.steps,
                                    "solve_passes_per_step": phases["solve_passes"] / max(phases["steps"], 1),
                                    "lowv_solves_per_step": phases["lowv_solves"] / max(phases["steps"], 1),

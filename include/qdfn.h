@@ -184,7 +184,10 @@ int qdfn_kernels_per_run(const qdfn_ctx* ctx);
  * patch solves, [9] their secant iterations (summed over patches, instances
  * (padding instances included) and solve passes); [10] ns of [2] that the
  * first block spent on its own solves and block reduction, [11] ns of [2] it
- * waited at the grid barrier after them. */
+ * waited at the grid barrier after them; [12]/[13] ns the first block's
+ * operator warps / solver warps spent in the overlapped operator-and-solve
+ * phase (FP32/BF16 dense operator), [14]/[15] the same for the slowest block of
+ * each step. */
 int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */

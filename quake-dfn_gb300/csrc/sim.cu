@@ -37,7 +37,7 @@ constexpr int kGranule = 8;                 // operator bytes per thread and sou
 constexpr int kMaxInst = 4;
 constexpr int kRedSlots = 8;                // doubles per (CTA, instance) partial
 constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
-constexpr int kCounters = 12;               // qdfn_get_counters slots
+constexpr int kCounters = 16;               // qdfn_get_counters slots
 
 // ---------------------------------------------------------------------------
 // matrix element formats: each thread owns VEC consecutive receiver rows, one
@@ -85,13 +85,18 @@ struct SimParams {
     const void* E;
     const void* Kn;
     hmat::Ops h;                     // H-matrix operator (hmat != 0)
-    int nchunk;                      // column chunks of the matvec
+    int nchunk;                      // column chunks of the matvec per row block
     int64_t chunk_len;
+    // the row blocks from rb_small0 on (streamed last) use nchunk2 chunks of
+    // chunk_len2 columns: smaller tiles at the end of the stream even out the
+    // blocks' finishing times and shrink the last row blocks' solve tail
+    int nchunk2;
+    int64_t chunk_len2, rb_small0;
     // state [R][N]
     double *V, *D, *theta, *fric, *accel, *sig_old;
     double *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
     int *instab, *flag, *sw;
-    double *part_s, *part_n;         // [nchunk][R][N]
+    double *part_s, *part_n;         // [max(nchunk, nchunk2)][R][N]
     // scalars [R]
     double *T, *dt;
     int64_t *step, *nrec;
@@ -102,9 +107,13 @@ struct SimParams {
     unsigned *bar_count, *bar_gen;
     double* red;                     // [2][nblocks][R][kRedSlots]
     unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
+    unsigned* rb_done;               // dense: column chunks finished per row block (this step)
+    unsigned long long* solve_ctr;   // dense: row chunks handed to the solver warps (this step)
     int* gerr;
     uint64_t budget_ns;             // wall-time budget of this launch
-    unsigned long long* prof;       // [8] cumulative counters (qdfn_get_counters)
+    unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
+    int64_t n_rb;                    // dense: operator row blocks
+    unsigned long long* tmax;        // [2][2] per-step max over blocks of (operator end, solver end), ns
 };
 
 // bounded grid barrier; returns false on timeout (all CTAs then return)
@@ -167,15 +176,19 @@ __device__ void block_reduce(double (&v)[kMaxInst][K], const int (&ops)[K], int 
             if (lane == 0) s_buf[wid][r][k] = x;
         }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // across warps: one thread per (instance, field), then thread 0 gathers
+    __shared__ unsigned long long s_out[kMaxInst][K];
+    if (threadIdx.x < R * K) {
+        const int r = threadIdx.x / K, k = threadIdx.x % K;
+        unsigned long long x = s_buf[0][r][k];
+        for (int w = 1; w < kSimThreads / 32; ++w) x = key_op(ops[k], x, s_buf[w][r][k]);
+        s_out[r][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                unsigned long long x = s_buf[0][r][k];
-                for (int w = 1; w < kSimThreads / 32; ++w) x = key_op(ops[k], x, s_buf[w][r][k]);
-                v[r][k] = ord_val(x);
-            }
-    }
+            for (int k = 0; k < K; ++k) v[r][k] = ord_val(s_out[r][k]);
     __syncthreads();
 }
 
@@ -218,10 +231,12 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 // products are summed in FP32 over 32 columns and folded error-free into
 // (hi, lo) FP32 pairs; FP64 storage accumulates in FP64.
 static_assert(hmat::kTileRows == kSimThreads, "H-matrix row tiles are one row per thread");
+constexpr int kOpWarps = 8;                                     // operator role: warps [0, kOpWarps)
+constexpr int kOpThreads = kOpWarps * 32;
 constexpr int kStages = 3;
-constexpr int kColsPerStage = 8;
+constexpr int kColsPerStage = 16;
 constexpr int kFoldStages = 32 / kColsPerStage;                 // FP32 sums span 32 columns
-constexpr int kSegBytes = kSimThreads * kGranule;               // one column of a row block, 4 KB
+constexpr int kSegBytes = kOpThreads * kGranule;                // one column of a row block, 2 KB
 constexpr int kStageBytes = 2 * kColsPerStage * kSegBytes;      // E and Kn, 64 KB
 constexpr int kPipeBytes = kStages * kStageBytes;               // 192 KB
 constexpr int kMbarBytes = 128;
@@ -272,6 +287,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, uint64_t
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// barrier of the operator role alone (named barrier 1, warps [0, kOpWarps))
+__device__ __forceinline__ void op_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kOpThreads) : "memory"); }
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* ptr) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+    return v;
+}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
@@ -296,7 +318,7 @@ __device__ __forceinline__ void pipe_init(Pipe& pp, unsigned char* smem) {
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(pp.full + s, 1);
-            mbar_init(pp.empty + s, kSimThreads / 32);
+            mbar_init(pp.empty + s, kOpWarps);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -341,17 +363,22 @@ __device__ __forceinline__ void xload(const X* p, X x[R]) {
 // pair; the hi parts are gathered error-free with TwoSum and the lo parts
 // added, all on the FP32 pipe, and the pair becomes a double once per row.
 // Loads are issued eight chunks at a time so they overlap.
+__device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
+    return rb >= p.rb_small0 ? p.nchunk2 : p.nchunk;
+}
+
 template <bool kPairs>
 __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t i, double& ss,
                                              double& sn) {
     const int64_t cs = (int64_t)p.R * p.N;
     const int64_t base = (int64_t)r * p.N + i;
+    const int nch = chunks_of_rb(p, i / p.ld);
     if constexpr (kPairs) {
         const float2* ps = reinterpret_cast<const float2*>(p.part_s) + base;
         const float2* pn = reinterpret_cast<const float2*>(p.part_n) + base;
         float hs = 0.f, ls = 0.f, hn = 0.f, ln = 0.f;
         int c = 0;
-        for (; c + 8 <= p.nchunk; c += 8) {
+        for (; c + 8 <= nch; c += 8) {
             float2 ts[8], tn[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
@@ -361,7 +388,7 @@ __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t 
                 two_sum_acc(hn, ln, tn[k].x); ln += tn[k].y;
             }
         }
-        for (; c < p.nchunk; ++c) {
+        for (; c < nch; ++c) {
             const float2 a = __ldcg(ps + c * cs), b = __ldcg(pn + c * cs);
             two_sum_acc(hs, ls, a.x); ls += a.y;
             two_sum_acc(hn, ln, b.x); ln += b.y;
@@ -373,14 +400,14 @@ __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t 
         const double* pn = p.part_n + base;
         double as = 0, an = 0;
         int c = 0;
-        for (; c + 8 <= p.nchunk; c += 8) {
+        for (; c + 8 <= nch; c += 8) {
             double ts[8], tn[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
 #pragma unroll
             for (int k = 0; k < 8; ++k) { as += ts[k]; an += tn[k]; }
         }
-        for (; c < p.nchunk; ++c) { as += __ldcg(ps + c * cs); an += __ldcg(pn + c * cs); }
+        for (; c < nch; ++c) { as += __ldcg(ps + c * cs); an += __ldcg(pn + c * cs); }
         ss = as;
         sn = an;
     }
@@ -391,10 +418,12 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int EB = kGranule / VEC;   // bytes per stored entry
-    constexpr int64_t rows_per_blk = (int64_t)kSimThreads * VEC;
+    constexpr int64_t rows_per_blk = (int64_t)kOpThreads * VEC;
     const int64_t N = p.N;
     const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
-    const int64_t ntiles = nrb * p.nchunk;
+    const int64_t nrb_big = min(p.rb_small0, nrb);
+    const int64_t T1 = nrb_big * p.nchunk;
+    const int64_t ntiles = T1 + (nrb - nrb_big) * p.nchunk2;
     const unsigned char* Eb = reinterpret_cast<const unsigned char*>(p.E);
     const unsigned char* Kb = reinterpret_cast<const unsigned char*>(p.Kn);
     __shared__ long long s_tile;
@@ -405,12 +434,16 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
         // CTAs that drew cheap tiles take more; results do not depend on the
         // assignment because every tile writes its own partial slot
         if (threadIdx.x == 0) s_tile = (long long)atomicAdd(p.tile_ctr, 1ull);
-        __syncthreads();
+        op_sync();
         const int64_t tile = s_tile;
         if (tile >= ntiles) break;
-        const int64_t rb = tile % nrb, c = tile / nrb;
-        const int64_t j0 = c * p.chunk_len;
-        const int64_t L = min(N, j0 + p.chunk_len) - j0;
+        // row-block-major order: the row blocks complete one after another, and
+        // the solver warps start on each as soon as its last chunk is in
+        int64_t rb, c, clen;
+        if (tile < T1) { rb = tile / p.nchunk; c = tile % p.nchunk; clen = p.chunk_len; }
+        else { rb = nrb_big + (tile - T1) / p.nchunk2; c = (tile - T1) % p.nchunk2; clen = p.chunk_len2; }
+        const int64_t j0 = c * clen;
+        const int64_t L = min(N, j0 + clen) - j0;
         const int64_t r0 = rb * rows_per_blk;
         const int nst = (int)((L + kColsPerStage - 1) / kColsPerStage);
         const uint32_t base = pp.consumed;
@@ -436,12 +469,12 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
             for (; issued < min(kStages, nst); ++issued) fill(issued);
         }
         // x of this chunk, the R instances of one column side by side
-        for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kSimThreads) {
+        for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kOpThreads) {
             const int r = (int)(q / L);
             const int64_t j = q % L;
             xs[j * R + r] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
         }
-        __syncthreads();
+        op_sync();
         const int64_t i0 = r0 + (int64_t)threadIdx.x * VEC;
         // FP64 storage: fs/fn are the accumulators.  FP32 storage: fs/fn sum
         // kFoldStages stages, then fold error-free into the pairs (h, l).
@@ -510,7 +543,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
             }
         }
         pp.consumed = base + nst;
-        __syncthreads();
+        op_sync();
         if (s_abort) {
             // drain the copies still in flight: the last fill of each slot (bounded)
             if (threadIdx.x == 0) {
@@ -520,7 +553,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
                     mbar_wait(pp.full + (n % kStages), (n / kStages) & 1u, kWaitLimitNs);
                 }
             }
-            __syncthreads();
+            op_sync();
             return false;
         }
         if (i0 < N) {
@@ -541,6 +574,11 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
                     }
                 }
         }
+        // publish the tile: every writer fences its partials, then one
+        // increment of the row block's completion count
+        __threadfence();
+        op_sync();
+        if (threadIdx.x == 0) atomicAdd(p.rb_done + rb, 1u);
     }
     return true;
 }
@@ -564,6 +602,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     // phase timers of CTA 0 (all CTAs leave each barrier together)
     uint64_t tp[4] = {0, 0, 0, 0}, tmark = globaltimer_ns();
     uint64_t tq[2] = {0, 0};   // P3 split: own items + block reduce / grid barrier wait
+    uint64_t tf[2] = {0, 0};   // dense P2: operator warps' time / solver warps' time
+    uint64_t tg[2] = {0, 0};   // the same, slowest block of each step
     unsigned long long n_iter = 0, n_steps = 0;
     unsigned long long n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations
     auto lap = [&](int k) { const uint64_t t = globaltimer_ns(); tp[k] += t - tmark; tmark = t; };
@@ -612,7 +652,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
                     s[4] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
                 }
-                if (blockIdx.x == 0) atomicExch(p.tile_ctr, 0ull);  // last used before the previous barrier
+                if (blockIdx.x == 0) {   // counters last used before the previous barrier
+                    atomicExch(p.tile_ctr, 0ull);
+                    if (!HM) atomicExch(p.solve_ctr, 0ull);
+                }
+            }
+            if (!HM && blockIdx.x == 0) {
+                for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) p.rb_done[k] = 0u;
+                if (threadIdx.x < 2) p.tmax[(it & 1) * 2 + threadIdx.x] = 0ull;   // read two steps ago
+                __threadfence();
             }
             if (!grid_barrier(p, deadline)) return;
             if ((threadIdx.x >> 5) < R) {
@@ -645,83 +693,166 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (stop) break;
         }
         lap(0);
+        // per-thread outcome of a solve pass: min flag, min Dt, any instability 4, min error
+        double v[kMaxInst][4];
+        auto v_init = [&]() {
+            for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
+        };
+        // one (instance r, patch i) item of a solve pass; pass 0 of a step also
+        // forms the row's operator products
+        auto solve_item = [&](int64_t q, int r, int64_t i, bool first) {
+            if (first) {
+                if constexpr (HM) {
+                    // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
+                    const double ss = hmat::row_sum<R>(p.h, 0, N, i, r);
+                    p.tld[q] = (-ss) / -p.kself[i];
+                    p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
+                } else {
+                    double ss, sn;
+                    sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
+                    p.tld[q] = -ss;   // ELSM * (0 - DispOld)
+                    p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
+                }
+            }
+            const double Dt = s_dt[r];
+            double dsn = 0, dss = 0, dsp = 0;
+            if (p.n_ext > 0) {
+                const double tq = p.interp_at_told ? s_T[r] : s_T[r] + Dt;
+                sim::interp_ext(p.n_ext, p.ext_t, p.ext_n, p.ext_s, p.ext_p, N, i, tq, dsn, dss, dsp);
+            }
+            double sig = p.knd[q] + p.sigma0[q] + dsn;
+            if (sig < p.sigma_min) sig = p.sigma_min;
+            if (i < Ns) {
+                sim::PatchIn pin;
+                pin.DispOld = p.D[q]; pin.FrictionOld = p.fric[q]; pin.ThetaOld = p.theta[q];
+                pin.VOld = p.V[q]; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
+                pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
+                pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
+                pin.dtau = dss; pin.sigma_old = p.sig_old[q]; pin.tau0 = p.tau0[q];
+                int err = 0;
+                const sim::PatchOut o = p.sw[q] == 1
+                    ? sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err)
+                    : sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
+                p.Vn[q] = o.V; p.fn[q] = o.Friction; p.Dn[q] = o.Disp; p.thn[q] = o.Theta;
+                p.sn[q] = sig; p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
+                if (p.sw[q] == 1) { ++n_hi; it_hi += o.Iterations; }
+                else { ++n_lo; it_lo += o.Iterations; }
+                if (err) v[r][3] = fmin(v[r][3], (double)err);
+                v[r][0] = fmin(v[r][0], (double)o.Flag);
+                v[r][1] = fmin(v[r][1], o.Dt);
+                if (o.Instab == 4) v[r][2] = 1;
+                if (o.Flag == 0) {   // Main_D :242-249, applied by the patch's owner
+                    if (o.Instab == 3) p.sw[q] = 1;
+                    else if (o.Instab == 4) p.sw[q] = 0;
+                }
+            } else {                 // loading faults (Solvers :370-377)
+                const double Vc = p.Vconst[q];
+                p.Vn[q] = Vc; p.fn[q] = p.fric[q]; p.Dn[q] = p.D[q] + Vc * Dt;
+                p.thn[q] = p.theta[q]; p.sn[q] = 1e10; p.dtall[q] = Dt;
+                p.instab[q] = 0; p.flag[q] = 1;
+                v[r][1] = fmin(v[r][1], Dt);
+            }
+        };
+        v_init();
         // ---------------------------------------------------------- P2
         if constexpr (HM) {
             hmat::pass_a<X, R>(p.h, p.D, N, xs, hacc);
             if (!grid_barrier(p, deadline)) return;
             hmat::pass_b<X, R>(p.h, p.D, N, xs);
+            if (!grid_barrier(p, deadline)) return;
+        } else if constexpr (sizeof(X) == 8) {
+            // FP64 storage: the operator's FMAs already load the FP64 pipe that
+            // the solves need, so the phases run one after the other
+            __shared__ int s_op_fail;
+            if (threadIdx.x == 0) s_op_fail = 0;
+            __syncthreads();
+            const uint64_t t_f0 = globaltimer_ns();
+            if ((threadIdx.x >> 5) < kOpWarps && !dense_matvec<M, R>(p, pipe, xs)) s_op_fail = 1;
+            if (threadIdx.x == 0) tf[0] += globaltimer_ns() - t_f0;
+            __syncthreads();
+            if (s_op_fail) return;
+            if (!grid_barrier(p, deadline)) return;
         } else {
-            if (!dense_matvec<M, R>(p, pipe, xs)) return;
+            // Operator and solve pass 0, overlapped.  Warps [0, kOpWarps) stream
+            // the operator tiles (HBM-bound); the other warps take 32-row chunks
+            // of every row block whose column chunks are all in and solve them
+            // (FP64-bound), so the two share each SM; the operator warps join
+            // the solving once the tiles are gone.  A row's solve needs only its
+            // own operator products, so the result is the same as running the
+            // phases one after the other.
+            __shared__ int s_fused_fail;
+            __shared__ unsigned long long s_t_solve;
+            if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; }
+            __syncthreads();
+            const uint64_t t_f0 = globaltimer_ns();
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            bool solve = true;
+            if (warp < kOpWarps) {
+                if (!dense_matvec<M, R>(p, pipe, xs)) { s_fused_fail = 1; solve = false; }
+                if (threadIdx.x == 0) {
+                    const uint64_t d = globaltimer_ns() - t_f0;
+                    tf[0] += d;
+                    atomicMax(p.tmax + (it & 1) * 2, (unsigned long long)d);
+                }
+            }
+            if (solve) {
+                constexpr int64_t rpb = (int64_t)kOpThreads * M::VEC;   // operator row block
+                constexpr int64_t cpr = rpb / 32;                        // row chunks per block and instance
+                const int64_t nk = p.n_rb * R * cpr;
+                for (;;) {
+                    unsigned long long k = 0;
+                    if (lane == 0) k = atomicAdd(p.solve_ctr, 1ull);
+                    k = __shfl_sync(0xffffffffu, k, 0);
+                    if ((int64_t)k >= nk) break;
+                    const int64_t rb = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
+                    const int r = (int)(rem / cpr);
+                    const int64_t i = rb * rpb + (rem % cpr) * 32 + lane;
+                    int ok = 1;
+                    if (lane == 0) {   // bounded wait for the row block's last column chunk
+                        const unsigned need = (unsigned)chunks_of_rb(p, rb);
+                        if (ld_acquire_u32(p.rb_done + rb) < need) {
+                            const uint64_t t0 = globaltimer_ns();
+                            while (ld_acquire_u32(p.rb_done + rb) < need) {
+                                if (globaltimer_ns() - t0 > kWaitLimitNs) { ok = 0; break; }
+                                __nanosleep(256);
+                            }
+                        }
+                    }
+                    ok = __shfl_sync(0xffffffffu, ok, 0);
+                    if (!ok) {
+                        if (lane == 0) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+                        s_fused_fail = 1;
+                        break;
+                    }
+                    if (i < N && !s_done[r]) solve_item((int64_t)r * N + i, r, i, true);
+                }
+                if (lane == 0) atomicMax(&s_t_solve, (unsigned long long)(globaltimer_ns() - t_f0));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tf[1] += s_t_solve;
+                atomicMax(p.tmax + (it & 1) * 2 + 1, s_t_solve);
+            }
+            if (s_fused_fail) return;
         }
-        if (!grid_barrier(p, deadline)) return;
         lap(1);
         // ---------------------------------------------------------- P3
         if (threadIdx.x == 0) s_iter = 0;
         __syncthreads();
         uint64_t tmark_p3 = globaltimer_ns();
         for (;;) {
-            double v[kMaxInst][4];
-            for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
             const int first = (s_iter == 0);
-            // every CTA takes an equal contiguous range of (instance, patch)
-            // items: the solves are FP64-pipe bound, so the per-SM item count
-            // sets the phase time
-            const int64_t per_cta = ((int64_t)R * N + gridDim.x - 1) / gridDim.x;
-            const int64_t q_end = min((int64_t)R * N, (int64_t)blockIdx.x * per_cta + per_cta);
-            for (int64_t q = (int64_t)blockIdx.x * per_cta + threadIdx.x; q < q_end; q += kSimThreads) {
-                const int r = (int)(q / N);
-                if (s_done[r]) continue;
-                const int64_t i = q - (int64_t)r * N;
-                if (first) {
-                    if constexpr (HM) {
-                        // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
-                        const double ss = hmat::row_sum<R>(p.h, 0, N, i, r);
-                        p.tld[q] = (-ss) / -p.kself[i];
-                        p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
-                    } else {
-                        double ss, sn;
-                        sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
-                        p.tld[q] = -ss;   // ELSM * (0 - DispOld)
-                        p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
-                    }
-                }
-                const double Dt = s_dt[r];
-                double dsn = 0, dss = 0, dsp = 0;
-                if (p.n_ext > 0) {
-                    const double tq = p.interp_at_told ? s_T[r] : s_T[r] + Dt;
-                    sim::interp_ext(p.n_ext, p.ext_t, p.ext_n, p.ext_s, p.ext_p, N, i, tq, dsn, dss, dsp);
-                }
-                double sig = p.knd[q] + p.sigma0[q] + dsn;
-                if (sig < p.sigma_min) sig = p.sigma_min;
-                if (i < Ns) {
-                    sim::PatchIn pin;
-                    pin.DispOld = p.D[q]; pin.FrictionOld = p.fric[q]; pin.ThetaOld = p.theta[q];
-                    pin.VOld = p.V[q]; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
-                    pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
-                    pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
-                    pin.dtau = dss; pin.sigma_old = p.sig_old[q]; pin.tau0 = p.tau0[q];
-                    int err = 0;
-                    const sim::PatchOut o = p.sw[q] == 1
-                        ? sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err)
-                        : sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
-                    p.Vn[q] = o.V; p.fn[q] = o.Friction; p.Dn[q] = o.Disp; p.thn[q] = o.Theta;
-                    p.sn[q] = sig; p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
-                    if (p.sw[q] == 1) { ++n_hi; it_hi += o.Iterations; }
-                    else { ++n_lo; it_lo += o.Iterations; }
-                    if (err) v[r][3] = fmin(v[r][3], (double)err);
-                    v[r][0] = fmin(v[r][0], (double)o.Flag);
-                    v[r][1] = fmin(v[r][1], o.Dt);
-                    if (o.Instab == 4) v[r][2] = 1;
-                    if (o.Flag == 0) {   // Main_D :242-249, applied by the patch's owner
-                        if (o.Instab == 3) p.sw[q] = 1;
-                        else if (o.Instab == 4) p.sw[q] = 0;
-                    }
-                } else {                 // loading faults (Solvers :370-377)
-                    const double Vc = p.Vconst[q];
-                    p.Vn[q] = Vc; p.fn[q] = p.fric[q]; p.Dn[q] = p.D[q] + Vc * Dt;
-                    p.thn[q] = p.theta[q]; p.sn[q] = 1e10; p.dtall[q] = Dt;
-                    p.instab[q] = 0; p.flag[q] = 1;
-                    v[r][1] = fmin(v[r][1], Dt);
+            if (HM || sizeof(X) == 8 || !first) {   // FP32/BF16 dense pass 0 ran alongside the operator
+                v_init();
+                // every CTA takes an equal contiguous range of (instance, patch)
+                // items: the solves are FP64-pipe bound, so the per-SM item count
+                // sets the pass time
+                const int64_t per_cta = ((int64_t)R * N + gridDim.x - 1) / gridDim.x;
+                const int64_t q_end = min((int64_t)R * N, (int64_t)blockIdx.x * per_cta + per_cta);
+                for (int64_t q = (int64_t)blockIdx.x * per_cta + threadIdx.x; q < q_end; q += kSimThreads) {
+                    const int r = (int)(q / N);
+                    if (s_done[r]) continue;
+                    solve_item(q, r, q - (int64_t)r * N, first != 0);
                 }
             }
             const int ops[4] = {1, 1, 0, 1};
@@ -738,6 +869,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 tq[0] += t_items - tmark_p3;
                 tq[1] += t - t_items;
                 tmark_p3 = t;
+                if (!HM && first && blockIdx.x == 0 && threadIdx.x == 0) {   // every block has stored its max
+                    tg[0] += __ldcg(p.tmax + (it & 1) * 2);
+                    tg[1] += __ldcg(p.tmax + (it & 1) * 2 + 1);
+                }
             }
             if ((threadIdx.x >> 5) < R) {
                 const int r = threadIdx.x >> 5;
@@ -818,6 +953,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         atomicAdd(p.prof + 5, n_steps);
         atomicAdd(p.prof + 10, (unsigned long long)tq[0]);
         atomicAdd(p.prof + 11, (unsigned long long)tq[1]);
+        atomicAdd(p.prof + 12, (unsigned long long)tf[0]);
+        atomicAdd(p.prof + 13, (unsigned long long)tf[1]);
+        atomicAdd(p.prof + 14, (unsigned long long)tg[0]);
+        atomicAdd(p.prof + 15, (unsigned long long)tg[1]);
     }
     if (p.prof) {   // solver work of every thread, one atomic per warp and counter
         unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};
@@ -845,6 +984,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
     using X = typename M::X;
     Pipe pipe;
     pipe_init(pipe, smem_raw);
+    if ((threadIdx.x >> 5) >= kOpWarps) return;   // the operator role alone
     dense_matvec<M, R>(p, pipe, reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes));
 }
 
@@ -954,12 +1094,15 @@ struct qdfn_ctx {
     int* gerr;
     unsigned long long* prof;
     unsigned long long* tile_ctr;
+    unsigned long long* solve_ctr;
+    unsigned* rb_done;
+    unsigned long long* tmax;
     void* E = nullptr;
     void* Kn = nullptr;
     int64_t n_ext = 0;
     double *ext_t = nullptr, *ext_n = nullptr, *ext_s = nullptr, *ext_p = nullptr;
-    int nblocks = 0, nblocks_override = 0, nchunk = 1;
-    int64_t chunk_len = 0;
+    int nblocks = 0, nblocks_override = 0, nchunk = 1, nchunk2 = 1;
+    int64_t chunk_len = 0, chunk_len2 = 0, rb_small0 = 0;
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1010,6 +1153,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.unstable = c->unstable; p.has_unstable = c->has_unstable;
     p.n_ext = c->n_ext; p.ext_t = c->ext_t; p.ext_n = c->ext_n; p.ext_s = c->ext_s; p.ext_p = c->ext_p;
     p.E = c->E; p.Kn = c->Kn; p.nchunk = c->nchunk; p.chunk_len = c->chunk_len;
+    p.nchunk2 = c->nchunk2; p.chunk_len2 = c->chunk_len2; p.rb_small0 = c->rb_small0;
     p.V = c->V; p.D = c->D; p.theta = c->theta; p.fric = c->fric; p.accel = c->accel; p.sig_old = c->sig_old;
     p.Vn = c->Vn; p.Dn = c->Dn; p.thn = c->thn; p.fn = c->fn; p.sn = c->sn; p.dtall = c->dtall;
     p.tld = c->tld; p.knd = c->knd; p.instab = c->instab; p.flag = c->flag; p.sw = c->sw;
@@ -1019,6 +1163,10 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
     p.prof = c->prof;
     p.tile_ctr = c->tile_ctr;
+    p.solve_ctr = c->solve_ctr;
+    p.rb_done = c->rb_done;
+    p.tmax = c->tmax;
+    p.n_rb = c->ld > 0 ? (c->N + c->ld - 1) / c->ld : 0;
     p.h = c->hops;
     p.budget_ns = budget_ns;
     return p;
@@ -1073,13 +1221,13 @@ int configure_launch(qdfn_ctx* c) {
     int64_t want_blocks;
     if (c->hmat) {
         c->smem = (size_t)Rk * hmat::kChunk * xsz + (size_t)hmat::kMaxRank * Rk * sizeof(double);
-        c->nchunk = 0;
-        c->chunk_len = 0;
+        c->nchunk = c->nchunk2 = 0;
+        c->chunk_len = c->chunk_len2 = c->rb_small0 = 0;
         want_blocks = std::max<int64_t>(c->hops.n_tiles, c->hops.n_lr);
     } else {
         // column chunks of at most 2048 sources staged in shared memory per instance,
         // enough (row block, chunk) tiles for >= 2 per SM
-        const int64_t rows_per_blk = (int64_t)kSimThreads * vec;
+        const int64_t rows_per_blk = (int64_t)kOpThreads * vec;
         const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
         int64_t want_chunks = std::max<int64_t>(1, (6LL * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
@@ -1088,8 +1236,13 @@ int configure_launch(qdfn_ctx* c) {
         clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), std::min<int64_t>(2048, cmax)) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
+        // half-width tiles for the row blocks of the last two waves of tiles
+        c->chunk_len2 = std::max<int64_t>(8, ((clen + 1) / 2 + 7) / 8 * 8);
+        c->nchunk2 = (int)((c->N + c->chunk_len2 - 1) / c->chunk_len2);
+        const int64_t nsmall = std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
+        c->rb_small0 = nrb - nsmall;
         c->smem = (size_t)kPipeBytes + kMbarBytes + (size_t)Rk * clen * xsz;
-        want_blocks = nrb * c->nchunk;
+        want_blocks = (nrb - nsmall) * c->nchunk + nsmall * c->nchunk2;
     }
     QDFN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
     int occ = 0;
@@ -1116,8 +1269,9 @@ int configure_launch(qdfn_ctx* c) {
     c->part_s = c->part_n = nullptr;
     int rc;
     if (!c->hmat) {
-        if ((rc = c->dalloc(&c->part_s, (size_t)c->nchunk * Rk * c->N))) return rc;
-        if ((rc = c->dalloc(&c->part_n, (size_t)c->nchunk * Rk * c->N))) return rc;
+        const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
+        if ((rc = c->dalloc(&c->part_s, slots * Rk * c->N))) return rc;
+        if ((rc = c->dalloc(&c->part_n, slots * Rk * c->N))) return rc;
     }
     if ((rc = c->dalloc(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots))) return rc;
     return QDFN_OK;
@@ -1153,6 +1307,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
     A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, kCounters); A(tile_ctr, 1);
+    A(solve_ctr, 1); A(tmax, 4); A(rb_done, (size_t)(N + kOpThreads - 1) / kOpThreads);   // row blocks of >= kOpThreads rows
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
@@ -1222,7 +1377,7 @@ int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t 
     c->hmat = 0;
     // ld holds the tile height (rows per block): 16 bytes per thread row group
     const size_t esz = precision == QDFN_FP64 ? 8 : 4;
-    c->ld = (int64_t)kSimThreads * (int64_t)(kGranule / esz);
+    c->ld = (int64_t)kOpThreads * (int64_t)(kGranule / esz);   // operator row block
     const int64_t nrows = (N + c->ld - 1) / c->ld * c->ld;
     const size_t mbytes = (size_t)N * nrows * esz;
     unsigned char *dE = nullptr, *dK = nullptr;
