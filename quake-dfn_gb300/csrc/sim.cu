@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -84,6 +85,8 @@ struct SimParams {
     // dense operator, source-major: entry (recv i, src j) at j*ld + i
     const void* E;
     const void* Kn;
+    void* xd;                        // dense: D in the operator's x type, [patch][instance], padded
+    int64_t xbuf;                    // dense: elements of one of the two shared-memory x buffers
     hmat::Ops h;                     // H-matrix operator (hmat != 0)
     int nchunk;                      // column chunks of the matvec per row block
     int64_t chunk_len;
@@ -116,7 +119,8 @@ struct SimParams {
     unsigned long long* tmax;        // [2][2] per-step max over blocks of (operator end, solver end), ns
 };
 
-// bounded grid barrier; returns false on timeout (all CTAs then return)
+// bounded grid barrier; returns false on timeout, or as soon as another block
+// has raised the error flag (all CTAs then return)
 __device__ bool grid_barrier(const SimParams& p, uint64_t deadline_ns) {
     __shared__ int s_ok;
     __syncthreads();
@@ -132,7 +136,10 @@ __device__ bool grid_barrier(const SimParams& p, uint64_t deadline_ns) {
             atomicAdd((unsigned*)p.bar_gen, 1u);
         } else {
             while (*gen == my_gen) {
-                if (globaltimer_ns() > deadline_ns + 2000000000ull) { ok = 0; break; }
+                if (globaltimer_ns() > deadline_ns + 2000000000ull || *(volatile int*)p.gerr != 0) {
+                    ok = 0;
+                    break;
+                }
                 __nanosleep(64);
             }
         }
@@ -233,6 +240,7 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 static_assert(hmat::kTileRows == kSimThreads, "H-matrix row tiles are one row per thread");
 constexpr int kOpWarps = 8;                                     // operator role: warps [0, kOpWarps)
 constexpr int kOpThreads = kOpWarps * 32;
+constexpr int kProducerWarp = kSimThreads / 32 - 1;             // lane 0 fills the stage ring
 constexpr int kStages = 3;
 constexpr int kColsPerStage = 16;
 constexpr int kFoldStages = 32 / kColsPerStage;                 // FP32 sums span 32 columns
@@ -287,6 +295,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, uint64_t
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// orders this thread's generic-proxy global writes (the x copy of D) with
+// later bulk-copy (async-proxy) reads of them
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 // barrier of the operator role alone (named barrier 1, warps [0, kOpWarps))
 __device__ __forceinline__ void op_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kOpThreads) : "memory"); }
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* ptr) {
@@ -299,22 +312,49 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
 }
 
-// pipeline state of one CTA: stage memory, the "full" mbarriers (completed by
-// the bulk copies' byte count), the "empty" mbarriers (one arrival per warp
-// once it has read the stage) and the number of stage fills consumed so far
-// (identical in every thread of the CTA)
+// Descriptor of the stage held by a ring slot.  The producer writes it before
+// the arrival that completes the slot's "full" barrier (release), consumers
+// read it after waiting on that barrier (acquire).
+struct StageDesc {
+    long long tile;   // operator tile, or -1: no tiles left (end marker)
+    int q, nst;       // stage index within the tile, stages of the tile
+    int seq;          // tile sequence number in this CTA (selects the x buffer)
+    int pad;
+};
+static_assert(6 * 8 + kStages * sizeof(StageDesc) <= kMbarBytes, "mbarriers + stage descriptors");
+
+// Pipeline state of one CTA: stage memory, the "full" mbarriers (completed by
+// the bulk copies' byte count), the "empty" mbarriers (one arrival per operator
+// warp once it has read the stage), the stage descriptors, and the running
+// stage counts.  `consumed` is identical in every operator thread; the
+// producer fields are used by thread 0 alone.  The ring keeps running across
+// tiles (the producer walks into the next tile as soon as a slot frees up) and
+// across steps.
 struct Pipe {
     unsigned char* stages;
     uint64_t* full;
     uint64_t* empty;
+    StageDesc* desc;
     uint32_t consumed;
+    // producer (thread 0)
+    uint32_t filled;
+    long long ftile;         // tile being filled; -2 none yet, -1 no tiles left
+    int fq, fnst, fseq;      // its next stage, its stage count, its sequence number
+    uint32_t last_stage[2];  // last stage of the latest tile using each x buffer
 };
+constexpr uint32_t kNoStage = 0xffffffffu;
 
 __device__ __forceinline__ void pipe_init(Pipe& pp, unsigned char* smem) {
     pp.stages = smem;
     pp.full = reinterpret_cast<uint64_t*>(smem + kPipeBytes);
     pp.empty = pp.full + kStages;
+    pp.desc = reinterpret_cast<StageDesc*>(pp.full + 2 * kStages);
     pp.consumed = 0;
+    pp.filled = 0;
+    pp.ftile = -2;
+    pp.fq = pp.fnst = 0;
+    pp.fseq = -1;
+    pp.last_stage[0] = pp.last_stage[1] = kNoStage;
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(pp.full + s, 1);
@@ -413,172 +453,225 @@ __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t 
     }
 }
 
+// Operator tile geometry: tile index -> (row block, column chunk, first
+// column, column count, stage count).  Row-block-major; the row blocks from
+// rb_small0 on use the half-width chunks.
+struct TileGeo {   // 32-bit: N < 2^31
+    int rb, c, j0, L, nst;
+};
+__device__ __forceinline__ TileGeo tile_geo(const SimParams& p, int64_t nrb, int64_t tile) {
+    const int64_t nrb_big = min(p.rb_small0, nrb);
+    const int64_t T1 = nrb_big * p.nchunk;
+    TileGeo g;
+    int64_t clen;
+    if (tile < T1) { g.rb = (int)(tile / p.nchunk); g.c = (int)(tile % p.nchunk); clen = p.chunk_len; }
+    else { g.rb = (int)(nrb_big + (tile - T1) / p.nchunk2); g.c = (int)((tile - T1) % p.nchunk2); clen = p.chunk_len2; }
+    g.j0 = (int)(g.c * clen);
+    g.L = (int)(min(p.N, (int64_t)g.j0 + clen) - g.j0);
+    g.nst = (g.L + kColsPerStage - 1) / kColsPerStage;
+    return g;
+}
+
+// Producer (thread 0): fill the next stage of the ring -- the next stage of the
+// tile being filled, the first stage of the next tile from the global counter
+// (with the tile's x chunk, from the instance-interleaved copy of D, in the
+// same transaction), or the end marker.  Returns false when a bounded wait
+// ran out.
 template <class M, int R>
-__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
+__device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, typename M::X* xs, int64_t nrb,
+                              int64_t ntiles, uint64_t pol) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int EB = kGranule / VEC;   // bytes per stored entry
     constexpr int64_t rows_per_blk = (int64_t)kOpThreads * VEC;
-    const int64_t N = p.N;
-    const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
-    const int64_t nrb_big = min(p.rb_small0, nrb);
-    const int64_t T1 = nrb_big * p.nchunk;
-    const int64_t ntiles = T1 + (nrb - nrb_big) * p.nchunk2;
-    const unsigned char* Eb = reinterpret_cast<const unsigned char*>(p.E);
-    const unsigned char* Kb = reinterpret_cast<const unsigned char*>(p.Kn);
-    __shared__ long long s_tile;
-    __shared__ int s_abort;        // a bounded wait ran out in this tile
+    const uint32_t n = pp.filled;
+    const int slot = (int)(n % kStages);
+    // the stage this slot held last must be released by every operator warp
+    if (n >= (uint32_t)kStages && !mbar_wait(pp.empty + slot, ((n - kStages) / kStages) & 1u, kWaitLimitNs))
+        return false;
+    if (pp.ftile == -2 || (pp.ftile >= 0 && pp.fq >= pp.fnst)) {
+        const long long t = (long long)atomicAdd(p.tile_ctr, 1ull);
+        if (t >= ntiles) {
+            pp.ftile = -1;
+        } else {
+            pp.ftile = t;
+            pp.fq = 0;
+            pp.fnst = tile_geo(p, nrb, t).nst;
+            pp.fseq++;
+        }
+    }
+    StageDesc* d = pp.desc + slot;
+    uint64_t* m = pp.full + slot;
+    if (pp.ftile == -1) {              // end marker: completes the phase without bytes
+        d->tile = -1;
+        mbar_arrive(m);
+        pp.filled = n + 1;
+        return true;
+    }
+    const TileGeo g = tile_geo(p, nrb, pp.ftile);
+    const int q = pp.fq;
+    const int xb = pp.fseq & 1;
+    if (q == 0) {
+        // the x buffer was last read by the tile before the previous one; its
+        // last stage is released already unless that was within kStages stages
+        const uint32_t prev = pp.last_stage[xb];
+        if (prev != kNoStage && prev + kStages > n &&
+            !mbar_wait(pp.empty + (prev % kStages), (prev / kStages) & 1u, kWaitLimitNs))
+            return false;
+    }
+    d->tile = pp.ftile;
+    d->q = q;
+    d->nst = g.nst;
+    d->seq = pp.fseq;
+    const int nc = (int)min((int64_t)kColsPerStage, g.L - (int64_t)q * kColsPerStage);
+    const uint32_t bytes = (uint32_t)nc * kSegBytes;
+    // x: the tile's columns rounded up to 4 (the copy is padded past N)
+    const uint32_t xbytes = q == 0 ? (uint32_t)(((g.L + 3) / 4 * 4) * R * sizeof(X)) : 0u;
+    fence_proxy_async();
+    mbar_expect_tx(m, 2u * bytes + xbytes);
+    unsigned char* st = pp.stages + (size_t)slot * kStageBytes;
+    // tile-contiguous layout: the nc columns of this row block are one run of
+    // nc * kSegBytes in each matrix -> one bulk copy per matrix
+    const int64_t off = (((int64_t)g.rb * p.N + g.j0 + (int64_t)q * kColsPerStage) * rows_per_blk) * EB;
+    bulk_g2s(st, reinterpret_cast<const unsigned char*>(p.E) + off, bytes, m, pol);
+    bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, reinterpret_cast<const unsigned char*>(p.Kn) + off, bytes, m,
+             pol);
+    if (q == 0)
+        bulk_g2s(xs + (size_t)xb * p.xbuf, reinterpret_cast<const X*>(p.xd) + (int64_t)g.j0 * R, xbytes, m, pol);
+    if (q == g.nst - 1) pp.last_stage[xb] = n;
+    pp.fq = q + 1;
+    pp.filled = n + 1;
+    return true;
+}
+
+// Producer role (one lane of warp kProducerWarp): walk this step's tiles and
+// keep the ring full -- every fill waits only for the release of the slot's
+// previous stage by the operator warps -- until the end marker is issued.  On
+// a failed wait it drains the copies it issued (bounded) and returns false.
+template <class M, int R>
+__device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs) {
+    constexpr int64_t rows_per_blk = (int64_t)kOpThreads * M::VEC;
+    const int64_t nrb = (p.N + rows_per_blk - 1) / rows_per_blk;
+    const int64_t ntiles = min(p.rb_small0, nrb) * p.nchunk + (nrb - min(p.rb_small0, nrb)) * p.nchunk2;
     const uint64_t pol = l2_evict_first_policy();
-    for (;;) {
-        // tiles are handed out by a global counter (reset once per step), so
-        // CTAs that drew cheap tiles take more; results do not depend on the
-        // assignment because every tile writes its own partial slot
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(p.tile_ctr, 1ull);
-        op_sync();
-        const int64_t tile = s_tile;
-        if (tile >= ntiles) break;
-        // row-block-major order: the row blocks complete one after another, and
-        // the solver warps start on each as soon as its last chunk is in
-        int64_t rb, c, clen;
-        if (tile < T1) { rb = tile / p.nchunk; c = tile % p.nchunk; clen = p.chunk_len; }
-        else { rb = nrb_big + (tile - T1) / p.nchunk2; c = (tile - T1) % p.nchunk2; clen = p.chunk_len2; }
-        const int64_t j0 = c * clen;
-        const int64_t L = min(N, j0 + clen) - j0;
-        const int64_t r0 = rb * rows_per_blk;
-        const int nst = (int)((L + kColsPerStage - 1) / kColsPerStage);
-        const uint32_t base = pp.consumed;
-        auto fill = [&](int q) {   // thread 0 only
-            const int slot = (int)((base + q) % kStages);
-            uint64_t* m = pp.full + slot;
-            const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
-            // tile-contiguous layout: the nc columns of this row block are one
-            // run of nc * 4 KB in each matrix -> one bulk copy per matrix
-            const uint32_t bytes = (uint32_t)nc * kSegBytes;
-            mbar_expect_tx(m, 2u * bytes);
-            unsigned char* st = pp.stages + (size_t)slot * kStageBytes;
-            const int64_t off = ((rb * N + j0 + (int64_t)q * kColsPerStage) * rows_per_blk) * EB;
-            bulk_g2s(st, Eb + off, bytes, m, pol);
-            bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, Kb + off, bytes, m, pol);
-        };
-        // the counter read above was preceded by a barrier at which every
-        // thread had finished the previous tile's stages, x and partials
-        int issued = 0;                    // fills of this tile (thread 0)
-        if (threadIdx.x == 0) {
-            s_abort = 0;
-            fence_proxy_async();
-            for (; issued < min(kStages, nst); ++issued) fill(issued);
-        }
-        // x of this chunk, the R instances of one column side by side
-        for (int64_t q = threadIdx.x; q < (int64_t)R * L; q += kOpThreads) {
-            const int r = (int)(q / L);
-            const int64_t j = q % L;
-            xs[j * R + r] = (X)__ldcg(p.D + (int64_t)r * N + j0 + j);
-        }
-        op_sync();
-        const int64_t i0 = r0 + (int64_t)threadIdx.x * VEC;
-        // FP64 storage: fs/fn are the accumulators.  FP32 storage: fs/fn sum
-        // kFoldStages stages, then fold error-free into the pairs (h, l).
-        X fs[R][VEC], fn[R][VEC];
-        float hs[R][VEC], ls[R][VEC], hn[R][VEC], ln[R][VEC];
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-#pragma unroll
-            for (int v = 0; v < VEC; ++v) {
-                fs[r][v] = 0; fn[r][v] = 0;
-                hs[r][v] = 0.f; ls[r][v] = 0.f; hn[r][v] = 0.f; ln[r][v] = 0.f;
-            }
-        for (int q = 0; q < nst; ++q) {
-            const uint32_t n = base + q;
-            const int slot = (int)(n % kStages);
-            bool have = *(volatile int*)&s_abort == 0;
-            if (have && !mbar_wait(pp.full + slot, (n / kStages) & 1u, kWaitLimitNs)) {
-                *(volatile int*)&s_abort = 1;
-                have = false;
-            }
-            const int nc = (int)min((int64_t)kColsPerStage, L - (int64_t)q * kColsPerStage);
-            const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * kGranule;
-            if (have && i0 < N) {
-#pragma unroll
-                for (int cc = 0; cc < kColsPerStage; ++cc) {
-                    if (cc < nc) {
-                        X e[VEC], k[VEC], x[R];
-                        M::sload(st + (size_t)cc * kSegBytes, e);
-                        M::sload(st + (size_t)(kColsPerStage + cc) * kSegBytes, k);
-                        xload<X, R>(xs + ((int64_t)q * kColsPerStage + cc) * R, x);
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-#pragma unroll
-                            for (int v = 0; v < VEC; ++v) {
-                                fs[r][v] = fma(e[v], x[r], fs[r][v]);
-                                fn[r][v] = fma(k[v], x[r], fn[r][v]);
-                            }
-                    }
-                }
-                if constexpr (sizeof(X) == 4) {
-                    if ((q + 1) % kFoldStages == 0 || q == nst - 1) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-#pragma unroll
-                            for (int v = 0; v < VEC; ++v) {
-                                two_sum_acc(hs[r][v], ls[r][v], (float)fs[r][v]);
-                                two_sum_acc(hn[r][v], ln[r][v], (float)fn[r][v]);
-                                fs[r][v] = 0;
-                                fn[r][v] = 0;
-                            }
-                    }
-                }
-            }
-            // release the slot: one arrival per warp; thread 0 refills it once
-            // all warps have arrived, the others run ahead into filled stages
-            __syncwarp();
-            if ((threadIdx.x & 31) == 0) mbar_arrive(pp.empty + slot);
-            if (threadIdx.x == 0 && q + kStages < nst && *(volatile int*)&s_abort == 0) {
-                if (mbar_wait(pp.empty + slot, (n / kStages) & 1u, kWaitLimitNs)) {
-                    fence_proxy_async();
-                    fill(q + kStages);
-                    ++issued;
-                } else {
-                    *(volatile int*)&s_abort = 1;
-                }
-            }
-        }
-        pp.consumed = base + nst;
-        op_sync();
-        if (s_abort) {
-            // drain the copies still in flight: the last fill of each slot (bounded)
-            if (threadIdx.x == 0) {
-                atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
-                for (int q = max(0, issued - kStages); q < issued; ++q) {
-                    const uint32_t n = base + q;
-                    mbar_wait(pp.full + (n % kStages), (n / kStages) & 1u, kWaitLimitNs);
-                }
-            }
-            op_sync();
+    fence_proxy_async_global();
+    pp.ftile = -2;
+    while (pp.ftile != -1) {
+        if (!produce_stage<M, R>(p, pp, xs, nrb, ntiles, pol)) {
+            atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+            const uint32_t from = pp.filled > (uint32_t)kStages ? pp.filled - kStages : 0u;
+            for (uint32_t k = from; k < pp.filled; ++k)
+                mbar_wait(pp.full + (k % kStages), (k / kStages) & 1u, kWaitLimitNs);
             return false;
         }
-        if (i0 < N) {
+    }
+    return true;
+}
+
+// Operator role (warps [0, kOpWarps)): consume the stage ring tile after tile.
+// Each thread owns VEC receiver rows of the current tile's row block and
+// accumulates the products of all R instances; at a tile's last stage it
+// writes its partials, and each warp then counts itself into the row block's
+// completion counter (kOpWarps arrivals per tile).
+template <class M, int R>
+__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
+    using X = typename M::X;
+    constexpr int VEC = M::VEC;
+    constexpr int64_t rows_per_blk = (int64_t)kOpThreads * VEC;
+    const int64_t N = p.N;
+    const int64_t nrb = (N + rows_per_blk - 1) / rows_per_blk;
+    bool ok = true;
+    // FP64 storage: fs/fn are the accumulators.  FP32 storage: fs/fn sum
+    // kFoldStages stages, then fold error-free into the pairs (h, l).
+    X fs[R][VEC], fn[R][VEC];
+    float hs[R][VEC], ls[R][VEC], hn[R][VEC], ln[R][VEC];
+    TileGeo g{};
+    int64_t i0 = 0;
+    const X* xsb = xs;
+    while (ok) {
+        const uint32_t n = pp.consumed;
+        const int slot = (int)(n % kStages);
+        if (!mbar_wait(pp.full + slot, (n / kStages) & 1u, kWaitLimitNs)) { ok = false; break; }
+        const StageDesc d = pp.desc[slot];
+        if (d.q == 0 && d.tile >= 0) {   // a new tile
+            g = tile_geo(p, nrb, d.tile);
+            i0 = (int64_t)g.rb * rows_per_blk + (int64_t)threadIdx.x * VEC;
+            xsb = xs + (size_t)(d.seq & 1) * p.xbuf;
 #pragma unroll
             for (int r = 0; r < R; ++r)
 #pragma unroll
                 for (int v = 0; v < VEC; ++v) {
-                    const int64_t i = i0 + v;
-                    if (i < N) {
-                        const int64_t o = ((int64_t)c * R + r) * N + i;
-                        if constexpr (sizeof(X) == 8) {
-                            p.part_s[o] = fs[r][v];
-                            p.part_n[o] = fn[r][v];
-                        } else {   // the pair itself: no FP64 work in this phase
-                            reinterpret_cast<float2*>(p.part_s)[o] = make_float2(hs[r][v], ls[r][v]);
-                            reinterpret_cast<float2*>(p.part_n)[o] = make_float2(hn[r][v], ln[r][v]);
-                        }
-                    }
+                    fs[r][v] = 0; fn[r][v] = 0;
+                    hs[r][v] = 0.f; ls[r][v] = 0.f; hn[r][v] = 0.f; ln[r][v] = 0.f;
                 }
         }
-        // publish the tile: every writer fences its partials, then one
-        // increment of the row block's completion count
-        __threadfence();
-        op_sync();
-        if (threadIdx.x == 0) atomicAdd(p.rb_done + rb, 1u);
+        if (d.tile >= 0 && i0 < N) {
+            const int q = d.q;
+            const int nc = (int)min((int64_t)kColsPerStage, g.L - (int64_t)q * kColsPerStage);
+            const unsigned char* st = pp.stages + (size_t)slot * kStageBytes + (size_t)threadIdx.x * kGranule;
+#pragma unroll
+            for (int cc = 0; cc < kColsPerStage; ++cc) {
+                if (cc < nc) {
+                    X e[VEC], k[VEC], x[R];
+                    M::sload(st + (size_t)cc * kSegBytes, e);
+                    M::sload(st + (size_t)(kColsPerStage + cc) * kSegBytes, k);
+                    xload<X, R>(xsb + ((int64_t)q * kColsPerStage + cc) * R, x);
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) {
+                            fs[r][v] = fma(e[v], x[r], fs[r][v]);
+                            fn[r][v] = fma(k[v], x[r], fn[r][v]);
+                        }
+                }
+            }
+            if constexpr (sizeof(X) == 4) {
+                if ((q + 1) % kFoldStages == 0 || q == d.nst - 1) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) {
+                            two_sum_acc(hs[r][v], ls[r][v], (float)fs[r][v]);
+                            two_sum_acc(hn[r][v], ln[r][v], (float)fn[r][v]);
+                            fs[r][v] = 0;
+                            fn[r][v] = 0;
+                        }
+                }
+            }
+        }
+        // release the slot: one arrival per warp; the producer refills it once
+        // every warp has arrived, the other warps run ahead into filled stages
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) mbar_arrive(pp.empty + slot);
+        pp.consumed = n + 1;
+        if (d.tile < 0) break;             // end marker
+        if (d.q == d.nst - 1) {            // the tile is complete: partials, then publish
+            if (i0 < N) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) {
+                        const int64_t i = i0 + v;
+                        if (i < N) {
+                            const int64_t o = ((int64_t)g.c * R + r) * N + i;
+                            if constexpr (sizeof(X) == 8) {
+                                p.part_s[o] = fs[r][v];
+                                p.part_n[o] = fn[r][v];
+                            } else {   // the pair itself: no FP64 work in this phase
+                                reinterpret_cast<float2*>(p.part_s)[o] = make_float2(hs[r][v], ls[r][v]);
+                                reinterpret_cast<float2*>(p.part_n)[o] = make_float2(hn[r][v], ln[r][v]);
+                            }
+                        }
+                    }
+            }
+            __threadfence();
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) atomicAdd(p.rb_done + g.rb, 1u);
+        }
+    }
+    if (!ok) {   // the producer drains the copies it issued
+        atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+        return false;
     }
     return true;
 }
@@ -600,13 +693,18 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     // the stop decision common to all CTAs
     const uint64_t deadline = globaltimer_ns() + p.budget_ns;
     // phase timers of CTA 0 (all CTAs leave each barrier together)
-    uint64_t tp[4] = {0, 0, 0, 0}, tmark = globaltimer_ns();
-    uint64_t tq[2] = {0, 0};   // P3 split: own items + block reduce / grid barrier wait
-    uint64_t tf[2] = {0, 0};   // dense P2: operator warps' time / solver warps' time
-    uint64_t tg[2] = {0, 0};   // the same, slowest block of each step
+    // device counters kept by thread 0 in shared memory (no registers held
+    // across the phases): [0..3] phases, [4..5] P3 split, [6..7] operator /
+    // solver warps of the overlapped phase, [8..9] the same for the slowest
+    // block of each step, [10] running mark, [11] P3 mark
+    __shared__ unsigned long long s_tm[12];
+    if (threadIdx.x < 12) s_tm[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_tm[10] = globaltimer_ns();
     unsigned long long n_iter = 0, n_steps = 0;
-    unsigned long long n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations
-    auto lap = [&](int k) { const uint64_t t = globaltimer_ns(); tp[k] += t - tmark; tmark = t; };
+    unsigned n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations of this thread
+    auto lap = [&](int k) {
+        if (threadIdx.x == 0) { const uint64_t t = globaltimer_ns(); s_tm[k] += t - s_tm[10]; s_tm[10] = t; }
+    };
     const int64_t N = p.N, Ns = p.N - p.Nload;
     const int64_t nthreads = (int64_t)gridDim.x * kSimThreads;
     const int64_t gtid = (int64_t)blockIdx.x * kSimThreads + threadIdx.x;
@@ -619,6 +717,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         s_fail[threadIdx.x] = p.status[threadIdx.x];
     }
     if (threadIdx.x == 0) s_stop = 0;
+    if constexpr (!HM) {   // the operator's copy of D (read by bulk copies after the first barrier)
+        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+            const int r = (int)(q / N);
+            reinterpret_cast<X*>(p.xd)[(q - (int64_t)r * N) * R + r] = (X)p.D[q];
+        }
+        fence_proxy_async_global();
+    }
     __syncthreads();
     auto red_slot = [&](int ph, int64_t blk, int r) -> double* {
         return p.red + (((int64_t)(ph & 1) * gridDim.x + blk) * R + r) * kRedSlots;
@@ -753,7 +858,6 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 v[r][1] = fmin(v[r][1], Dt);
             }
         };
-        v_init();
         // ---------------------------------------------------------- P2
         if constexpr (HM) {
             hmat::pass_a<X, R>(p.h, p.D, N, xs, hacc);
@@ -767,8 +871,12 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (threadIdx.x == 0) s_op_fail = 0;
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
-            if ((threadIdx.x >> 5) < kOpWarps && !dense_matvec<M, R>(p, pipe, xs)) s_op_fail = 1;
-            if (threadIdx.x == 0) tf[0] += globaltimer_ns() - t_f0;
+            if ((threadIdx.x >> 5) < kOpWarps) {
+                if (!dense_matvec<M, R>(p, pipe, xs)) s_op_fail = 1;
+            } else if (threadIdx.x == kProducerWarp * 32) {
+                if (!produce_tiles<M, R>(p, pipe, xs)) s_op_fail = 1;
+            }
+            if (threadIdx.x == 0) s_tm[6] += globaltimer_ns() - t_f0;
             __syncthreads();
             if (s_op_fail) return;
             if (!grid_barrier(p, deadline)) return;
@@ -791,11 +899,17 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 if (!dense_matvec<M, R>(p, pipe, xs)) { s_fused_fail = 1; solve = false; }
                 if (threadIdx.x == 0) {
                     const uint64_t d = globaltimer_ns() - t_f0;
-                    tf[0] += d;
+                    s_tm[6] += d;
                     atomicMax(p.tmax + (it & 1) * 2, (unsigned long long)d);
                 }
+            } else if (warp == kProducerWarp) {   // lane 0 fills the ring, then the warp solves
+                int pok = 1;
+                if (lane == 0) pok = produce_tiles<M, R>(p, pipe, xs) ? 1 : 0;
+                pok = __shfl_sync(0xffffffffu, pok, 0);
+                if (!pok) { s_fused_fail = 1; solve = false; }
             }
             if (solve) {
+                v_init();
                 constexpr int64_t rpb = (int64_t)kOpThreads * M::VEC;   // operator row block
                 constexpr int64_t cpr = rpb / 32;                        // row chunks per block and instance
                 const int64_t nk = p.n_rb * R * cpr;
@@ -809,11 +923,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     const int64_t i = rb * rpb + (rem % cpr) * 32 + lane;
                     int ok = 1;
                     if (lane == 0) {   // bounded wait for the row block's last column chunk
-                        const unsigned need = (unsigned)chunks_of_rb(p, rb);
+                        const unsigned need = (unsigned)chunks_of_rb(p, rb) * kOpWarps;   // one per warp and tile
                         if (ld_acquire_u32(p.rb_done + rb) < need) {
                             const uint64_t t0 = globaltimer_ns();
                             while (ld_acquire_u32(p.rb_done + rb) < need) {
-                                if (globaltimer_ns() - t0 > kWaitLimitNs) { ok = 0; break; }
+                                if (globaltimer_ns() - t0 > kWaitLimitNs || *(volatile int*)p.gerr != 0) {
+                                    ok = 0;
+                                    break;
+                                }
                                 __nanosleep(256);
                             }
                         }
@@ -830,16 +947,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                tf[1] += s_t_solve;
+                s_tm[7] += s_t_solve;
                 atomicMax(p.tmax + (it & 1) * 2 + 1, s_t_solve);
             }
             if (s_fused_fail) return;
         }
         lap(1);
         // ---------------------------------------------------------- P3
-        if (threadIdx.x == 0) s_iter = 0;
+        if (threadIdx.x == 0) { s_iter = 0; s_tm[11] = globaltimer_ns(); }
         __syncthreads();
-        uint64_t tmark_p3 = globaltimer_ns();
         for (;;) {
             const int first = (s_iter == 0);
             if (HM || sizeof(X) == 8 || !first) {   // FP32/BF16 dense pass 0 ran alongside the operator
@@ -862,16 +978,18 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     double* s = red_slot(phase, blockIdx.x, r);
                     s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
                 }
-            const uint64_t t_items = globaltimer_ns();
+            const uint64_t t_items = threadIdx.x == 0 ? globaltimer_ns() : 0;
             if (!grid_barrier(p, deadline)) return;
             {   // CTA 0: own solves + block reduction, then the wait for the grid
-                const uint64_t t = globaltimer_ns();
-                tq[0] += t_items - tmark_p3;
-                tq[1] += t - t_items;
-                tmark_p3 = t;
+                if (threadIdx.x == 0) {
+                    const uint64_t t = globaltimer_ns();
+                    s_tm[4] += t_items - s_tm[11];
+                    s_tm[5] += t - t_items;
+                    s_tm[11] = t;
+                }
                 if (!HM && first && blockIdx.x == 0 && threadIdx.x == 0) {   // every block has stored its max
-                    tg[0] += __ldcg(p.tmax + (it & 1) * 2);
-                    tg[1] += __ldcg(p.tmax + (it & 1) * 2 + 1);
+                    s_tm[8] += __ldcg(p.tmax + (it & 1) * 2);
+                    s_tm[9] += __ldcg(p.tmax + (it & 1) * 2 + 1);
                 }
             }
             if ((threadIdx.x >> 5) < R) {
@@ -929,6 +1047,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             }
             p.accel[q] = (p.Vn[q] - p.V[q]) / Dt;
             p.D[q] = p.Dn[q];
+            if constexpr (!HM) {
+                reinterpret_cast<X*>(p.xd)[i * R + r] = (X)p.Dn[q];
+                fence_proxy_async_global();
+            }
             p.theta[q] = p.thn[q];
             p.V[q] = p.Vn[q];
             p.fric[q] = p.fn[q];
@@ -948,18 +1070,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         n_steps++;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.prof) {
-        for (int k = 0; k < 4; ++k) atomicAdd(p.prof + k, (unsigned long long)tp[k]);
+        for (int k = 0; k < 4; ++k) atomicAdd(p.prof + k, s_tm[k]);
         atomicAdd(p.prof + 4, n_iter);
         atomicAdd(p.prof + 5, n_steps);
-        atomicAdd(p.prof + 10, (unsigned long long)tq[0]);
-        atomicAdd(p.prof + 11, (unsigned long long)tq[1]);
-        atomicAdd(p.prof + 12, (unsigned long long)tf[0]);
-        atomicAdd(p.prof + 13, (unsigned long long)tf[1]);
-        atomicAdd(p.prof + 14, (unsigned long long)tg[0]);
-        atomicAdd(p.prof + 15, (unsigned long long)tg[1]);
+        for (int k = 0; k < 6; ++k) atomicAdd(p.prof + 10 + k, s_tm[4 + k]);
     }
     if (p.prof) {   // solver work of every thread, one atomic per warp and counter
-        unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};
+        unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};   // widened before the sums
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             for (int o = 16; o > 0; o >>= 1) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
@@ -977,6 +1094,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     }
 }
 
+// x copy of D for the operator-only kernel: [patch][instance] in the operator's type
+template <class X, int R>
+__global__ void k_fill_xd(SimParams p) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (int64_t)R * p.N) return;
+    const int r = (int)(q / p.N);
+    reinterpret_cast<X*>(p.xd)[(q - (int64_t)r * p.N) * R + r] = (X)p.D[q];
+}
+
 // Operator-only kernel (qdfn_apply_operator): one pass of P2 + chunk reduction.
 template <class M, int R>
 __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
@@ -984,8 +1110,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
     using X = typename M::X;
     Pipe pipe;
     pipe_init(pipe, smem_raw);
-    if ((threadIdx.x >> 5) >= kOpWarps) return;   // the operator role alone
-    dense_matvec<M, R>(p, pipe, reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes));
+    X* xs = reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes);
+    const int warp = threadIdx.x >> 5;
+    if (warp < kOpWarps) dense_matvec<M, R>(p, pipe, xs);          // the operator role
+    else if (threadIdx.x == kProducerWarp * 32) produce_tiles<M, R>(p, pipe, xs);
 }
 
 template <class X, int R>
@@ -1103,6 +1231,8 @@ struct qdfn_ctx {
     double *ext_t = nullptr, *ext_n = nullptr, *ext_s = nullptr, *ext_p = nullptr;
     int nblocks = 0, nblocks_override = 0, nchunk = 1, nchunk2 = 1;
     int64_t chunk_len = 0, chunk_len2 = 0, rb_small0 = 0;
+    void* xd = nullptr;              // x copy of D (dense)
+    int64_t xbuf = 0;                // elements per shared-memory x buffer
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1153,6 +1283,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.unstable = c->unstable; p.has_unstable = c->has_unstable;
     p.n_ext = c->n_ext; p.ext_t = c->ext_t; p.ext_n = c->ext_n; p.ext_s = c->ext_s; p.ext_p = c->ext_p;
     p.E = c->E; p.Kn = c->Kn; p.nchunk = c->nchunk; p.chunk_len = c->chunk_len;
+    p.xd = c->xd; p.xbuf = c->xbuf;
     p.nchunk2 = c->nchunk2; p.chunk_len2 = c->chunk_len2; p.rb_small0 = c->rb_small0;
     p.V = c->V; p.D = c->D; p.theta = c->theta; p.fric = c->fric; p.accel = c->accel; p.sig_old = c->sig_old;
     p.Vn = c->Vn; p.Dn = c->Dn; p.thn = c->thn; p.fn = c->fn; p.sn = c->sn; p.dtall = c->dtall;
@@ -1229,10 +1360,13 @@ int configure_launch(qdfn_ctx* c) {
         // enough (row block, chunk) tiles for >= 2 per SM
         const int64_t rows_per_blk = (int64_t)kOpThreads * vec;
         const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
-        int64_t want_chunks = std::max<int64_t>(1, (6LL * sms + nrb - 1) / nrb);
+        // tiles per SM and step before the guided tail (tuning knob QDFN_TILES_PER_SM)
+        int64_t tiles_per_sm = 3;
+        if (const char* e = std::getenv("QDFN_TILES_PER_SM")) tiles_per_sm = std::max(1, std::min(64, std::atoi(e)));
+        int64_t want_chunks = std::max<int64_t>(1, (tiles_per_sm * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
-        // x staging (R x chunk x elem) shares the 227 KB with the 192 KB stage ring
-        const int64_t cmax = std::max<int64_t>(64, (int64_t)(30 * 1024) / (Rk * (int64_t)xsz));
+        // two x buffers (R x chunk x elem each) share the 227 KB with the 192 KB stage ring
+        const int64_t cmax = std::max<int64_t>(64, (int64_t)(15 * 1024) / (Rk * (int64_t)xsz));
         clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), std::min<int64_t>(2048, cmax)) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
@@ -1241,7 +1375,10 @@ int configure_launch(qdfn_ctx* c) {
         c->nchunk2 = (int)((c->N + c->chunk_len2 - 1) / c->chunk_len2);
         const int64_t nsmall = std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
         c->rb_small0 = nrb - nsmall;
-        c->smem = (size_t)kPipeBytes + kMbarBytes + (size_t)Rk * clen * xsz;
+        // one x buffer: the chunk's columns rounded up to 4 (bulk copies move
+        // multiples of 16 bytes), in 128-byte units
+        c->xbuf = (((clen + 3) / 4 * 4) * Rk * (int64_t)xsz + 127) / 128 * 128 / (int64_t)xsz;
+        c->smem = (size_t)kPipeBytes + kMbarBytes + 2 * (size_t)c->xbuf * xsz;
         want_blocks = (nrb - nsmall) * c->nchunk + nsmall * c->nchunk2;
     }
     QDFN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
@@ -1269,6 +1406,10 @@ int configure_launch(qdfn_ctx* c) {
     c->part_s = c->part_n = nullptr;
     int rc;
     if (!c->hmat) {
+        c->release(c->xd);
+        c->xd = nullptr;
+        // x copy of D: N columns padded to a multiple of 8 (+8), read in runs of 4
+        if ((rc = c->dalloc(reinterpret_cast<unsigned char**>(&c->xd), ((size_t)c->N + 16) * Rk * xsz))) return rc;
         const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
         if ((rc = c->dalloc(&c->part_s, slots * Rk * c->N))) return rc;
         if ((rc = c->dalloc(&c->part_n, slots * Rk * c->N))) return rc;
@@ -1595,6 +1736,16 @@ extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, do
         QDFN_CUDA(cudaGetLastError());
     } else {
         QDFN_CUDA(cudaMemset(c->tile_ctr, 0, sizeof(unsigned long long)));
+        const unsigned fb = (unsigned)((tot + 255) / 256);
+        switch ((c->prec == QDFN_FP64 ? 10 : 0) + kernel_R(c->R)) {
+            case 1: k_fill_xd<float, 1><<<fb, 256>>>(p); break;
+            case 2: k_fill_xd<float, 2><<<fb, 256>>>(p); break;
+            case 4: k_fill_xd<float, 4><<<fb, 256>>>(p); break;
+            case 11: k_fill_xd<double, 1><<<fb, 256>>>(p); break;
+            case 12: k_fill_xd<double, 2><<<fb, 256>>>(p); break;
+            default: k_fill_xd<double, 4><<<fb, 256>>>(p); break;
+        }
+        QDFN_CUDA(cudaGetLastError());
         apply_kernel(c->prec, c->R)<<<c->nblocks, kSimThreads, c->smem>>>(p);
         QDFN_CUDA(cudaGetLastError());
         if (c->prec == QDFN_FP64) k_chunk_reduce<false><<<(unsigned)((tot + 255) / 256), 256>>>(p);
