@@ -187,7 +187,9 @@ int qdfn_kernels_per_run(const qdfn_ctx* ctx);
  * waited at the grid barrier after them; [12]/[13] ns the first block's
  * operator warps / solver warps spent in the overlapped operator-and-solve
  * phase (FP32/BF16 dense operator), [14]/[15] the same for the slowest block of
- * each step. */
+ * each step, [16] the longest time from a row block being complete to one of
+ * its row chunks being solved, [17] the longest partial-sum time of a row
+ * (per-step maxima, summed over steps). */
 int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */

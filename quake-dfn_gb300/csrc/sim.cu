@@ -36,9 +36,9 @@ namespace {
 constexpr int kSimThreads = 512;
 constexpr int kGranule = 8;                 // operator bytes per thread and source column
 constexpr int kMaxInst = 4;
-constexpr int kRedSlots = 8;                // doubles per (CTA, instance) partial
+constexpr int kRedSlots = 16;               // doubles per (CTA, instance) partial
 constexpr int64_t kRetryCap = 10000;        // retries of one step before giving up
-constexpr int kCounters = 16;               // qdfn_get_counters slots
+constexpr int kCounters = 18;               // qdfn_get_counters slots
 
 // ---------------------------------------------------------------------------
 // matrix element formats: each thread owns VEC consecutive receiver rows, one
@@ -85,8 +85,10 @@ struct SimParams {
     // dense operator, source-major: entry (recv i, src j) at j*ld + i
     const void* E;
     const void* Kn;
-    void* xd;                        // dense: D in the operator's x type, [patch][instance], padded
+    void* xd;                        // dense: D in the operator's x type, [patch][instance], padded;
+                                     // two copies xd_stride elements apart (current / next step)
     int64_t xbuf;                    // dense: elements of one of the two shared-memory x buffers
+    int64_t xd_stride, rb_stride;    // element strides of the two x copies and row-block counter sets
     hmat::Ops h;                     // H-matrix operator (hmat != 0)
     int nchunk;                      // column chunks of the matvec per row block
     int64_t chunk_len;
@@ -96,9 +98,12 @@ struct SimParams {
     int nchunk2;
     int64_t chunk_len2, rb_small0;
     // state [R][N]
+    // state, two buffers swapped per accepted step: (V, D, theta, fric, accel,
+    // sig_old, sw) and (Vn, Dn, thn, fn, accel_n, sn, sw_n); the host sees the
+    // first set (the kernel copies back at its end when needed)
     double *V, *D, *theta, *fric, *accel, *sig_old;
-    double *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
-    int *instab, *flag, *sw;
+    double *Vn, *Dn, *thn, *fn, *sn, *accel_n, *dtall, *tld, *knd;
+    int *instab, *flag, *sw, *sw_n;
     double *part_s, *part_n;         // [max(nchunk, nchunk2)][R][N]
     // scalars [R]
     double *T, *dt;
@@ -109,14 +114,16 @@ struct SimParams {
     // barrier + reductions
     unsigned *bar_count, *bar_gen;
     double* red;                     // [2][nblocks][R][kRedSlots]
+    // per-step counters, [2] (and rb_done [2][rb_stride]) by step parity
     unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
-    unsigned* rb_done;               // dense: column chunks finished per row block (this step)
-    unsigned long long* solve_ctr;   // dense: row chunks handed to the solver warps (this step)
+    unsigned* rb_done;               // dense: tile arrivals per row block (one per operator warp and tile)
+    unsigned long long* solve_ctr;   // dense: row chunks handed to the solver warps
     int* gerr;
     uint64_t budget_ns;             // wall-time budget of this launch
     unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
     int64_t n_rb;                    // dense: operator row blocks
-    unsigned long long* tmax;        // [2][2] per-step max over blocks of (operator end, solver end), ns
+    unsigned long long* tmax;        // [2][4] per-step max over blocks of (operator end, solver end,
+                                     // chunk ready->solved, chunk partial sums), ns
 };
 
 // bounded grid barrier; returns false on timeout, or as soon as another block
@@ -479,7 +486,7 @@ __device__ __forceinline__ TileGeo tile_geo(const SimParams& p, int64_t nrb, int
 // ran out.
 template <class M, int R>
 __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, typename M::X* xs, int64_t nrb,
-                              int64_t ntiles, uint64_t pol) {
+                              int64_t ntiles, uint64_t pol, int cpar, const typename M::X* xdc) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int EB = kGranule / VEC;   // bytes per stored entry
@@ -490,7 +497,7 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     if (n >= (uint32_t)kStages && !mbar_wait(pp.empty + slot, ((n - kStages) / kStages) & 1u, kWaitLimitNs))
         return false;
     if (pp.ftile == -2 || (pp.ftile >= 0 && pp.fq >= pp.fnst)) {
-        const long long t = (long long)atomicAdd(p.tile_ctr, 1ull);
+        const long long t = (long long)atomicAdd(p.tile_ctr + cpar, 1ull);
         if (t >= ntiles) {
             pp.ftile = -1;
         } else {
@@ -537,7 +544,7 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, reinterpret_cast<const unsigned char*>(p.Kn) + off, bytes, m,
              pol);
     if (q == 0)
-        bulk_g2s(xs + (size_t)xb * p.xbuf, reinterpret_cast<const X*>(p.xd) + (int64_t)g.j0 * R, xbytes, m, pol);
+        bulk_g2s(xs + (size_t)xb * p.xbuf, xdc + (int64_t)g.j0 * R, xbytes, m, pol);
     if (q == g.nst - 1) pp.last_stage[xb] = n;
     pp.fq = q + 1;
     pp.filled = n + 1;
@@ -549,7 +556,8 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
 // previous stage by the operator warps -- until the end marker is issued.  On
 // a failed wait it drains the copies it issued (bounded) and returns false.
 template <class M, int R>
-__device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs) {
+__device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs, int cpar,
+                              const typename M::X* xdc) {
     constexpr int64_t rows_per_blk = (int64_t)kOpThreads * M::VEC;
     const int64_t nrb = (p.N + rows_per_blk - 1) / rows_per_blk;
     const int64_t ntiles = min(p.rb_small0, nrb) * p.nchunk + (nrb - min(p.rb_small0, nrb)) * p.nchunk2;
@@ -557,7 +565,7 @@ __device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs) {
     fence_proxy_async_global();
     pp.ftile = -2;
     while (pp.ftile != -1) {
-        if (!produce_stage<M, R>(p, pp, xs, nrb, ntiles, pol)) {
+        if (!produce_stage<M, R>(p, pp, xs, nrb, ntiles, pol, cpar, xdc)) {
             atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
             const uint32_t from = pp.filled > (uint32_t)kStages ? pp.filled - kStages : 0u;
             for (uint32_t k = from; k < pp.filled; ++k)
@@ -574,7 +582,7 @@ __device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs) {
 // writes its partials, and each warp then counts itself into the row block's
 // completion counter (kOpWarps arrivals per tile).
 template <class M, int R>
-__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
+__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, int cpar) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int64_t rows_per_blk = (int64_t)kOpThreads * VEC;
@@ -666,7 +674,7 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
             }
             __threadfence();
             __syncwarp();
-            if ((threadIdx.x & 31) == 0) atomicAdd(p.rb_done + g.rb, 1u);
+            if ((threadIdx.x & 31) == 0) atomicAdd(p.rb_done + cpar * p.rb_stride + g.rb, 1u);
         }
     }
     if (!ok) {   // the producer drains the copies it issued
@@ -676,29 +684,69 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs) {
     return true;
 }
 
+// Time control of the next step (Main_D :162-201) from the reduced statistics
+// of the current state: max V and NaN flag over the controlled set, min |V/A|,
+// whether any |V/A| was usable.  Returns the step size; *empty reports an
+// empty minimum (Julia's `minimum` of an empty set).
+__device__ __forceinline__ double next_dt(const SimParams& p, double vmax, double vnan, double dtmin, double any,
+                                          double dt_prev, bool* empty) {
+    *empty = (any == 0);
+    if (vnan != 0) vmax = NAN;
+    dtmin = dtmin / p.dt_cut;
+    double DtRef;
+    if (vmax > p.switch_v) DtRef = p.rupture_dt;
+    else if (dtmin > p.max_dt) DtRef = p.max_dt;
+    else DtRef = dtmin;
+    double Dt = dt_prev;
+    if (DtRef <= p.rupture_dt) Dt = DtRef;
+    else if (Dt < DtRef / 1.2) Dt = Dt * 1.2;
+    else Dt = DtRef;
+    return Dt;
+}
+
+// The two state buffers of the step loop; `cur` holds the state at the start
+// of a step, `nxt` receives the solves' results and becomes `cur` when the
+// step is accepted.
+struct StateView {
+    double *V, *D, *theta, *fric, *accel, *sig_old;
+    int* sw;
+};
+__device__ __forceinline__ StateView state_view(const SimParams& p, int which) {
+    if (which == 0) return {p.V, p.D, p.theta, p.fric, p.accel, p.sig_old, p.sw};
+    return {p.Vn, p.Dn, p.thn, p.fn, p.accel_n, p.sn, p.sw_n};
+}
+
 template <class M, int R, bool HM>
 __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nsteps) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using X = typename M::X;
-    // dense: [stage ring | mbarriers | x];  H-matrix: [x | rank accumulators]
+    // dense: [stage ring | mbarriers, stage descriptors | two x buffers];
+    // H-matrix: [x | rank accumulators]
     X* xs = reinterpret_cast<X*>(HM ? smem_raw : smem_raw + kPipeBytes + kMbarBytes);
     double* hacc = reinterpret_cast<double*>(smem_raw + (size_t)R * hmat::kChunk * sizeof(X));
     Pipe pipe;
     if constexpr (!HM) pipe_init(pipe, smem_raw);
-    __shared__ double s_T[kMaxInst], s_dt[kMaxInst];
+    // s_dt: Dt of the current step; s_dtn: the next step's, decided with the
+    // reductions of the current one; s_dta: the last accepted Dt (what the
+    // host keeps, and the next launch's controller starts from)
+    __shared__ double s_T[kMaxInst], s_dt[kMaxInst], s_dtn[kMaxInst], s_dta[kMaxInst];
     __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
-    __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop;
+    __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop, s_par;
     __shared__ int s_iter;
-    // each CTA measures the budget from its own start; the P1 reduction makes
-    // the stop decision common to all CTAs
+    // this block's reduction of a solve pass, as order-preserving keys (exact
+    // min/max, integer pipe), one set per instance: [0] min flag, [1] min Dt,
+    // [2] any instability 4, [3] min error; for the next step's time control
+    // [4] max V, [5] V is NaN, [6] min |V/A|, [7] any |V/A| usable
+    __shared__ unsigned long long s_red[kMaxInst][8];
+    // each CTA measures the budget from its own start; the reductions make the
+    // stop decision common to all CTAs
     const uint64_t deadline = globaltimer_ns() + p.budget_ns;
-    // phase timers of CTA 0 (all CTAs leave each barrier together)
     // device counters kept by thread 0 in shared memory (no registers held
     // across the phases): [0..3] phases, [4..5] P3 split, [6..7] operator /
     // solver warps of the overlapped phase, [8..9] the same for the slowest
-    // block of each step, [10] running mark, [11] P3 mark
-    __shared__ unsigned long long s_tm[12];
-    if (threadIdx.x < 12) s_tm[threadIdx.x] = 0;
+    // block of each step, [10] running mark, [11] P3 mark, [12..13] chunk maxima
+    __shared__ unsigned long long s_tm[14];
+    if (threadIdx.x < 14) s_tm[threadIdx.x] = 0;
     if (threadIdx.x == 0) s_tm[10] = globaltimer_ns();
     unsigned long long n_iter = 0, n_steps = 0;
     unsigned n_lo = 0, it_lo = 0, n_hi = 0, it_hi = 0;   // solves / secant iterations of this thread
@@ -712,100 +760,104 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     if (threadIdx.x < R) {
         s_T[threadIdx.x] = p.T[threadIdx.x];
         s_dt[threadIdx.x] = p.dt[threadIdx.x];
+        s_dta[threadIdx.x] = p.dt[threadIdx.x];
         s_step[threadIdx.x] = p.step[threadIdx.x];
         s_nrec[threadIdx.x] = p.nrec[threadIdx.x];
         s_fail[threadIdx.x] = p.status[threadIdx.x];
     }
-    if (threadIdx.x == 0) s_stop = 0;
-    if constexpr (!HM) {   // the operator's copy of D (read by bulk copies after the first barrier)
-        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
-            const int r = (int)(q / N);
-            reinterpret_cast<X*>(p.xd)[(q - (int64_t)r * N) * R + r] = (X)p.D[q];
-        }
-        fence_proxy_async_global();
-    }
-    __syncthreads();
+    if (threadIdx.x == 0) { s_stop = 0; s_par = 0; }
     auto red_slot = [&](int ph, int64_t blk, int r) -> double* {
         return p.red + (((int64_t)(ph & 1) * gridDim.x + blk) * R + r) * kRedSlots;
     };
+    auto red_init = [&]() {
+        if (threadIdx.x < R * 8) {
+            const int k = threadIdx.x % 8;
+            // neutral elements: min fields +inf, max fields -inf (flags start at 1 / 0)
+            const double v0[8] = {1.0, INFINITY, 0.0, 0.0, -INFINITY, 0.0, INFINITY, 0.0};
+            s_red[threadIdx.x / 8][k] = ord_key(v0[k]);
+        }
+    };
+    auto red_min = [&](int r, int k, double x) { atomicMin(&s_red[r][k], ord_key(x)); };
+    auto red_max = [&](int r, int k, double x) { atomicMax(&s_red[r][k], ord_key(x)); };
+
+    // ------------------------------------------------------------ prologue
+    // time control of the first step from the state as it stands (later steps
+    // take theirs from the solves that produce their state), the solver
+    // switches, the counters of step 0 and the operator's copy of D
+    {
+        double v[kMaxInst][4];
+        for (int r = 0; r < R; ++r) { v[r][0] = -INFINITY; v[r][1] = 0; v[r][2] = INFINITY; v[r][3] = 0; }
+        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+            const int r = (int)(q / N);
+            const int64_t i = q - (int64_t)r * N;
+            const double Vo = p.V[q];
+            p.sw[q] = Vo > p.switch_v ? 1 : 0;
+            if constexpr (!HM) reinterpret_cast<X*>(p.xd)[i * R + r] = (X)p.D[q];
+            const bool ctl = p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns);
+            if (ctl) {
+                if (isnan(Vo)) v[r][1] = 1;
+                else v[r][0] = fmax(v[r][0], Vo);
+                const double qa = fabs(Vo / p.accel[q]);
+                if (!isnan(qa) && qa != 0) { v[r][3] = 1; v[r][2] = fmin(v[r][2], qa); }
+            }
+        }
+        if constexpr (!HM) fence_proxy_async_global();
+        const int ops[4] = {0, 0, 1, 0};
+        block_reduce<4>(v, ops, R);
+        if (threadIdx.x == 0) {
+            for (int r = 0; r < R; ++r) {
+                double* s = red_slot(phase, blockIdx.x, r);
+                s[4] = v[r][0]; s[5] = v[r][1]; s[6] = v[r][2]; s[7] = v[r][3];
+                s[8] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
+            }
+            if (blockIdx.x == 0) { atomicExch(p.tile_ctr, 0ull); atomicExch(p.solve_ctr, 0ull); }
+        }
+        if (!HM && blockIdx.x == 0) {   // step 0's counter set
+            for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) p.rb_done[k] = 0u;
+            if (threadIdx.x < 4) p.tmax[threadIdx.x] = 0ull;
+            __threadfence();
+        }
+        if (!grid_barrier(p, deadline)) return;
+        if ((threadIdx.x >> 5) < R) {
+            const int r = threadIdx.x >> 5;
+            const int ops5[5] = {0, 0, 1, 0, 0};
+            double f[5];
+            grid_fields<5>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots + 4, gridDim.x, R, r, ops5, f);
+            if ((threadIdx.x & 31) == 0) {
+                if (f[4] != 0) s_stop = 1;   // benign race: every writer stores 1
+                bool empty;
+                s_dt[r] = next_dt(p, f[0], f[1], f[2], f[3], s_dt[r], &empty);
+                if (empty && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
+            }
+        }
+        phase++;
+        __syncthreads();
+    }
+    lap(0);
 
     for (int64_t it = 0; it < nsteps; ++it) {
-        // ---------------------------------------------------------- P1
         {
-            double v[kMaxInst][4];
-            int errloc = 0;
-            for (int r = 0; r < R; ++r) { v[r][0] = -INFINITY; v[r][1] = 0; v[r][2] = INFINITY; v[r][3] = 0; }
-            for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
-                const int r = (int)(q / N);
-                const int64_t i = q - (int64_t)r * N;
-                const double Vo = p.V[q];
-                p.sw[q] = Vo > p.switch_v ? 1 : 0;
-                const bool ctl = p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns);
-                if (ctl) {
-                    if (isnan(Vo)) v[r][1] = 1;
-                    else v[r][0] = fmax(v[r][0], Vo);
-                    const double qa = fabs(Vo / p.accel[q]);
-                    if (!isnan(qa) && qa != 0) { v[r][3] = 1; v[r][2] = fmin(v[r][2], qa); }
-                }
-            }
-            (void)errloc;
-            const int ops[4] = {0, 0, 1, 0};
-            block_reduce<4>(v, ops, R);
-            if (threadIdx.x == 0) {
-                for (int r = 0; r < R; ++r) {
-                    double* s = red_slot(phase, blockIdx.x, r);
-                    s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
-                    s[4] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
-                }
-                if (blockIdx.x == 0) {   // counters last used before the previous barrier
-                    atomicExch(p.tile_ctr, 0ull);
-                    if (!HM) atomicExch(p.solve_ctr, 0ull);
-                }
-            }
-            if (!HM && blockIdx.x == 0) {
-                for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) p.rb_done[k] = 0u;
-                if (threadIdx.x < 2) p.tmax[(it & 1) * 2 + threadIdx.x] = 0ull;   // read two steps ago
-                __threadfence();
-            }
-            if (!grid_barrier(p, deadline)) return;
-            if ((threadIdx.x >> 5) < R) {
-                const int r = threadIdx.x >> 5;
-                const int ops[5] = {0, 0, 1, 0, 0};
-                double f[5];
-                grid_fields<5>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r, ops, f);
-                double vmax = f[0], vnan = f[1], dtmin = f[2], any = f[3], late = f[4];
-                if ((threadIdx.x & 31) == 0) {
-                if (late != 0) s_stop = 1;   // benign race: every writer stores 1
-                if (vnan != 0) vmax = NAN;
-                if (any == 0 && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
-                dtmin = dtmin / p.dt_cut;
-                double DtRef;
-                if (vmax > p.switch_v) DtRef = p.rupture_dt;
-                else if (dtmin > p.max_dt) DtRef = p.max_dt;
-                else DtRef = dtmin;
-                double Dt = s_dt[r];
-                if (DtRef <= p.rupture_dt) Dt = DtRef;
-                else if (Dt < DtRef / 1.2) Dt = Dt * 1.2;
-                else Dt = DtRef;
-                s_dt[r] = Dt;
-                s_done[r] = 0;
-                }
-            }
-            phase++;
-            __syncthreads();
             int stop = s_stop;
             for (int r = 0; r < R; ++r) stop |= (s_fail[r] != 0);
             if (stop) break;
         }
-        lap(0);
-        // per-thread outcome of a solve pass: min flag, min Dt, any instability 4, min error
-        double v[kMaxInst][4];
-        auto v_init = [&]() {
-            for (int r = 0; r < R; ++r) { v[r][0] = 1; v[r][1] = INFINITY; v[r][2] = 0; v[r][3] = 0; }
-        };
+        const int par = s_par;             // which buffer holds the current state
+        const int cpar = (int)(it & 1);    // which counter set this step uses
+        if (threadIdx.x < R) s_done[threadIdx.x] = 0;
+        red_init();
+        __syncthreads();
+        const X* xdc = reinterpret_cast<const X*>(p.xd) + (size_t)par * p.xd_stride;
         // one (instance r, patch i) item of a solve pass; pass 0 of a step also
-        // forms the row's operator products
-        auto solve_item = [&](int64_t q, int r, int64_t i, bool first) {
+        // forms the row's operator products.  pair: the item runs on a lane
+        // pair (lanes 2k, 2k+1, both called with it); the even lane writes the
+        // results, the next step's solver switch and Accel, and this item's
+        // share of the step reductions.
+        uint64_t t_sp = 0;   // duration of the last item's partial sums (diagnostics)
+        // buffer pointers are selected where used, so none is held across the solve
+#define QDFN_CUR(a, b) (par ? p.b : p.a)
+#define QDFN_NXT(a, b) (par ? p.a : p.b)
+        auto solve_item = [&](int64_t q, int r, int64_t i, bool first, bool pair) {
+            const bool writer = !pair || (threadIdx.x & 1) == 0;
             if (first) {
                 if constexpr (HM) {
                     // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
@@ -814,9 +866,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
                 } else {
                     double ss, sn;
+                    const uint64_t t_sp0 = globaltimer_ns();
                     sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
-                    p.tld[q] = -ss;   // ELSM * (0 - DispOld)
-                    p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
+                    t_sp = globaltimer_ns() - t_sp0;
+                    if (writer) {
+                        p.tld[q] = -ss;   // ELSM * (0 - DispOld)
+                        p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
+                    }
+                    if (pair) __syncwarp(3u << (threadIdx.x & 30));   // the odd lane reads them below
                 }
             }
             const double Dt = s_dt[r];
@@ -827,42 +884,77 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             }
             double sig = p.knd[q] + p.sigma0[q] + dsn;
             if (sig < p.sigma_min) sig = p.sigma_min;
+            const double VOld = QDFN_CUR(V, Vn)[q];
+            double Vnew;
             if (i < Ns) {
                 sim::PatchIn pin;
-                pin.DispOld = p.D[q]; pin.FrictionOld = p.fric[q]; pin.ThetaOld = p.theta[q];
-                pin.VOld = p.V[q]; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
+                pin.DispOld = QDFN_CUR(D, Dn)[q]; pin.FrictionOld = QDFN_CUR(fric, fn)[q];
+                pin.ThetaOld = QDFN_CUR(theta, thn)[q];
+                pin.VOld = VOld; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
                 pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
                 pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
-                pin.dtau = dss; pin.sigma_old = p.sig_old[q]; pin.tau0 = p.tau0[q];
+                pin.dtau = dss; pin.sigma_old = QDFN_CUR(sig_old, sn)[q]; pin.tau0 = p.tau0[q];
                 int err = 0;
-                const sim::PatchOut o = p.sw[q] == 1
-                    ? sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err)
-                    : sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
-                p.Vn[q] = o.V; p.fn[q] = o.Friction; p.Dn[q] = o.Disp; p.thn[q] = o.Theta;
-                p.sn[q] = sig; p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
-                if (p.sw[q] == 1) { ++n_hi; it_hi += o.Iterations; }
-                else { ++n_lo; it_lo += o.Iterations; }
-                if (err) v[r][3] = fmin(v[r][3], (double)err);
-                v[r][0] = fmin(v[r][0], (double)o.Flag);
-                v[r][1] = fmin(v[r][1], o.Dt);
-                if (o.Instab == 4) v[r][2] = 1;
-                if (o.Flag == 0) {   // Main_D :242-249, applied by the patch's owner
-                    if (o.Instab == 3) p.sw[q] = 1;
-                    else if (o.Instab == 4) p.sw[q] = 0;
+                sim::PatchOut o;
+                const int swq = QDFN_CUR(sw, sw_n)[q];
+                if (swq == 1) {
+                    if (!writer) return;   // the high-velocity solver runs on one lane
+                    o = sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err);
+                } else if (pair) {
+                    o = sim::solve_lowv_t<true>(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
+                } else {
+                    o = sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
                 }
-            } else {                 // loading faults (Solvers :370-377)
+                if (!writer) return;
+                QDFN_NXT(V, Vn)[q] = o.V; QDFN_NXT(fric, fn)[q] = o.Friction; QDFN_NXT(D, Dn)[q] = o.Disp;
+                QDFN_NXT(theta, thn)[q] = o.Theta; QDFN_NXT(sig_old, sn)[q] = sig;
+                p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
+                if (swq == 1) { ++n_hi; it_hi += o.Iterations; }
+                else { ++n_lo; it_lo += o.Iterations; }
+                if (err) red_min(r, 3, (double)err);
+                if (o.Flag != 1) red_min(r, 0, (double)o.Flag);
+                red_min(r, 1, o.Dt);
+                if (o.Instab == 4) red_max(r, 2, 1.0);
+                if (o.Flag == 0) {   // Main_D :242-249, applied by the patch's owner
+                    if (o.Instab == 3) QDFN_CUR(sw, sw_n)[q] = 1;
+                    else if (o.Instab == 4) QDFN_CUR(sw, sw_n)[q] = 0;
+                }
+                Vnew = o.V;
+                if constexpr (!HM) reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)o.Disp;
+            } else {
+                if (!writer) return;   // loading faults (Solvers :370-377)
                 const double Vc = p.Vconst[q];
-                p.Vn[q] = Vc; p.fn[q] = p.fric[q]; p.Dn[q] = p.D[q] + Vc * Dt;
-                p.thn[q] = p.theta[q]; p.sn[q] = 1e10; p.dtall[q] = Dt;
+                const double Dn = QDFN_CUR(D, Dn)[q] + Vc * Dt;
+                QDFN_NXT(V, Vn)[q] = Vc; QDFN_NXT(fric, fn)[q] = QDFN_CUR(fric, fn)[q]; QDFN_NXT(D, Dn)[q] = Dn;
+                QDFN_NXT(theta, thn)[q] = QDFN_CUR(theta, thn)[q]; QDFN_NXT(sig_old, sn)[q] = 1e10;
+                p.dtall[q] = Dt;
                 p.instab[q] = 0; p.flag[q] = 1;
-                v[r][1] = fmin(v[r][1], Dt);
+                red_min(r, 1, Dt);
+                Vnew = Vc;
+                if constexpr (!HM) reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)Dn;
+            }
+            if constexpr (!HM) fence_proxy_async_global();
+            // the next step's Accel, solver switch and time-control statistics
+            // (Main_D :265-319 then :162-201) -- final once the step is accepted,
+            // since an accepted pass keeps its Dt
+            const double A = (Vnew - VOld) / Dt;
+            QDFN_NXT(accel, accel_n)[q] = A;
+            QDFN_NXT(sw, sw_n)[q] = Vnew > p.switch_v ? 1 : 0;
+            if (p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns)) {
+                if (isnan(Vnew)) red_max(r, 5, 1.0);
+                else red_max(r, 4, Vnew);
+                const double qa = fabs(Vnew / A);
+                if (!isnan(qa) && qa != 0) { red_max(r, 7, 1.0); red_min(r, 6, qa); }
             }
         };
+#undef QDFN_CUR
+#undef QDFN_NXT
         // ---------------------------------------------------------- P2
         if constexpr (HM) {
-            hmat::pass_a<X, R>(p.h, p.D, N, xs, hacc);
+            const double* Dcur = par ? p.Dn : p.D;
+            hmat::pass_a<X, R>(p.h, Dcur, N, xs, hacc);
             if (!grid_barrier(p, deadline)) return;
-            hmat::pass_b<X, R>(p.h, p.D, N, xs);
+            hmat::pass_b<X, R>(p.h, Dcur, N, xs);
             if (!grid_barrier(p, deadline)) return;
         } else if constexpr (sizeof(X) == 8) {
             // FP64 storage: the operator's FMAs already load the FP64 pipe that
@@ -872,9 +964,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
             if ((threadIdx.x >> 5) < kOpWarps) {
-                if (!dense_matvec<M, R>(p, pipe, xs)) s_op_fail = 1;
+                if (!dense_matvec<M, R>(p, pipe, xs, cpar)) s_op_fail = 1;
             } else if (threadIdx.x == kProducerWarp * 32) {
-                if (!produce_tiles<M, R>(p, pipe, xs)) s_op_fail = 1;
+                if (!produce_tiles<M, R>(p, pipe, xs, cpar, xdc)) s_op_fail = 1;
             }
             if (threadIdx.x == 0) s_tm[6] += globaltimer_ns() - t_f0;
             __syncthreads();
@@ -882,7 +974,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (!grid_barrier(p, deadline)) return;
         } else {
             // Operator and solve pass 0, overlapped.  Warps [0, kOpWarps) stream
-            // the operator tiles (HBM-bound); the other warps take 32-row chunks
+            // the operator tiles (HBM-bound); the other warps take 16-row chunks
             // of every row block whose column chunks are all in and solve them
             // (FP64-bound), so the two share each SM; the operator warps join
             // the solving once the tiles are gone.  A row's solve needs only its
@@ -896,37 +988,37 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
             bool solve = true;
             if (warp < kOpWarps) {
-                if (!dense_matvec<M, R>(p, pipe, xs)) { s_fused_fail = 1; solve = false; }
+                if (!dense_matvec<M, R>(p, pipe, xs, cpar)) { s_fused_fail = 1; solve = false; }
                 if (threadIdx.x == 0) {
                     const uint64_t d = globaltimer_ns() - t_f0;
                     s_tm[6] += d;
-                    atomicMax(p.tmax + (it & 1) * 2, (unsigned long long)d);
+                    atomicMax(p.tmax + cpar * 4, (unsigned long long)d);
                 }
             } else if (warp == kProducerWarp) {   // lane 0 fills the ring, then the warp solves
                 int pok = 1;
-                if (lane == 0) pok = produce_tiles<M, R>(p, pipe, xs) ? 1 : 0;
+                if (lane == 0) pok = produce_tiles<M, R>(p, pipe, xs, cpar, xdc) ? 1 : 0;
                 pok = __shfl_sync(0xffffffffu, pok, 0);
                 if (!pok) { s_fused_fail = 1; solve = false; }
             }
             if (solve) {
-                v_init();
                 constexpr int64_t rpb = (int64_t)kOpThreads * M::VEC;   // operator row block
-                constexpr int64_t cpr = rpb / 32;                        // row chunks per block and instance
+                constexpr int64_t cpr = rpb / 16;     // 16-row chunks (one lane pair per row) per block and instance
                 const int64_t nk = p.n_rb * R * cpr;
+                const unsigned* rbd = p.rb_done + cpar * p.rb_stride;
                 for (;;) {
                     unsigned long long k = 0;
-                    if (lane == 0) k = atomicAdd(p.solve_ctr, 1ull);
+                    if (lane == 0) k = atomicAdd(p.solve_ctr + cpar, 1ull);
                     k = __shfl_sync(0xffffffffu, k, 0);
                     if ((int64_t)k >= nk) break;
                     const int64_t rb = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
                     const int r = (int)(rem / cpr);
-                    const int64_t i = rb * rpb + (rem % cpr) * 32 + lane;
+                    const int64_t i = rb * rpb + (rem % cpr) * 16 + (lane >> 1);
                     int ok = 1;
                     if (lane == 0) {   // bounded wait for the row block's last column chunk
                         const unsigned need = (unsigned)chunks_of_rb(p, rb) * kOpWarps;   // one per warp and tile
-                        if (ld_acquire_u32(p.rb_done + rb) < need) {
+                        if (ld_acquire_u32(rbd + rb) < need) {
                             const uint64_t t0 = globaltimer_ns();
-                            while (ld_acquire_u32(p.rb_done + rb) < need) {
+                            while (ld_acquire_u32(rbd + rb) < need) {
                                 if (globaltimer_ns() - t0 > kWaitLimitNs || *(volatile int*)p.gerr != 0) {
                                     ok = 0;
                                     break;
@@ -941,14 +1033,19 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         s_fused_fail = 1;
                         break;
                     }
-                    if (i < N && !s_done[r]) solve_item((int64_t)r * N + i, r, i, true);
+                    const uint64_t t_ready = globaltimer_ns();
+                    if (i < N) solve_item((int64_t)r * N + i, r, i, true, true);
+                    if (lane == 0) {
+                        atomicMax(p.tmax + cpar * 4 + 2, (unsigned long long)(globaltimer_ns() - t_ready));
+                        atomicMax(p.tmax + cpar * 4 + 3, (unsigned long long)t_sp);
+                    }
                 }
                 if (lane == 0) atomicMax(&s_t_solve, (unsigned long long)(globaltimer_ns() - t_f0));
             }
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_tm[7] += s_t_solve;
-                atomicMax(p.tmax + (it & 1) * 2 + 1, s_t_solve);
+                atomicMax(p.tmax + cpar * 4 + 1, s_t_solve);
             }
             if (s_fused_fail) return;
         }
@@ -959,7 +1056,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         for (;;) {
             const int first = (s_iter == 0);
             if (HM || sizeof(X) == 8 || !first) {   // FP32/BF16 dense pass 0 ran alongside the operator
-                v_init();
+                if (!first) {
+                    red_init();
+                    __syncthreads();
+                }
                 // every CTA takes an equal contiguous range of (instance, patch)
                 // items: the solves are FP64-pipe bound, so the per-SM item count
                 // sets the pass time
@@ -968,16 +1068,27 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 for (int64_t q = (int64_t)blockIdx.x * per_cta + threadIdx.x; q < q_end; q += kSimThreads) {
                     const int r = (int)(q / N);
                     if (s_done[r]) continue;
-                    solve_item(q, r, q - (int64_t)r * N, first != 0);
+                    solve_item(q, r, q - (int64_t)r * N, first != 0, false);
                 }
             }
-            const int ops[4] = {1, 1, 0, 1};
-            block_reduce<4>(v, ops, R);
-            if (threadIdx.x == 0)
+            if (first && !HM && blockIdx.x == 0) {
+                // reset the other counter set for the next step: its last use was
+                // the previous step, which every block has left
+                if (threadIdx.x == 0) { atomicExch(p.tile_ctr + (cpar ^ 1), 0ull); atomicExch(p.solve_ctr + (cpar ^ 1), 0ull); }
+                unsigned* rbn = p.rb_done + (cpar ^ 1) * p.rb_stride;
+                for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) rbn[k] = 0u;
+                if (threadIdx.x < 4) p.tmax[(cpar ^ 1) * 4 + threadIdx.x] = 0ull;
+                __threadfence();
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const double late = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
                 for (int r = 0; r < R; ++r) {
                     double* s = red_slot(phase, blockIdx.x, r);
-                    s[0] = v[r][0]; s[1] = v[r][1]; s[2] = v[r][2]; s[3] = v[r][3];
+                    for (int k = 0; k < 8; ++k) s[k] = ord_val(s_red[r][k]);
+                    s[8] = late;
                 }
+            }
             const uint64_t t_items = threadIdx.x == 0 ? globaltimer_ns() : 0;
             if (!grid_barrier(p, deadline)) return;
             {   // CTA 0: own solves + block reduction, then the wait for the grid
@@ -988,25 +1099,31 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     s_tm[11] = t;
                 }
                 if (!HM && first && blockIdx.x == 0 && threadIdx.x == 0) {   // every block has stored its max
-                    s_tm[8] += __ldcg(p.tmax + (it & 1) * 2);
-                    s_tm[9] += __ldcg(p.tmax + (it & 1) * 2 + 1);
+                    s_tm[8] += __ldcg(p.tmax + cpar * 4);
+                    s_tm[9] += __ldcg(p.tmax + cpar * 4 + 1);
+                    s_tm[12] += __ldcg(p.tmax + cpar * 4 + 2);
+                    s_tm[13] += __ldcg(p.tmax + cpar * 4 + 3);
                 }
             }
             if ((threadIdx.x >> 5) < R) {
                 const int r = threadIdx.x >> 5;
                 if (!s_done[r]) {
-                    const int ops[4] = {1, 1, 0, 1};
-                    double f[4];
-                    grid_fields<4>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r, ops,
+                    const int ops[9] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
+                    double f[9];
+                    grid_fields<9>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r, ops,
                                    f);
                     const double mflag = f[0], mdt = f[1], any4 = f[2], err = f[3];
                     if ((threadIdx.x & 31) == 0) {
+                        if (f[8] != 0) s_stop = 1;   // benign race: every writer stores 1
                         if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
                         else if (mflag == 0) {
                             s_dt[r] = any4 != 0 ? 1e-3 : mdt;
                         } else {
                             s_dt[r] = mdt;   // Main_D :262 Dt = minimum(Dt_All)
                             s_done[r] = 1;
+                            bool empty;      // the next step's Dt from this state
+                            s_dtn[r] = next_dt(p, f[4], f[5], f[6], f[7], mdt, &empty);
+                            if (empty && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
                         }
                     }
                 }
@@ -1025,36 +1142,36 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 break;
             }
         }
-        {
-            int anyfail = 0;
-            for (int r = 0; r < R; ++r) anyfail |= (s_fail[r] != 0);
-            if (anyfail) break;
+        {   // an instance that failed in its solves keeps the state it had
+            int solvefail = 0;
+            for (int r = 0; r < R; ++r) solvefail |= (s_fail[r] != 0 && s_fail[r] != QDFN_ERR_EMPTY);
+            if (solvefail) break;
         }
         lap(2);
         // ---------------------------------------------------------- P4
-        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
-            const int r = (int)(q / N);
-            const int64_t i = q - (int64_t)r * N;
-            const double Dt = s_dt[r];
-            const int64_t gstep = s_step[r] + 1;
-            if (p.record_step > 0 && gstep % p.record_step == 0 && s_nrec[r] < p.max_records) {
-                const int64_t o = ((int64_t)r * p.max_records + s_nrec[r]) * N + i;
-                p.hV[o] = p.Vn[q]; p.hD[o] = p.Dn[q]; p.hth[o] = p.thn[q]; p.hs[o] = p.sn[q];
-                if (i == 0) {
-                    p.hT[(int64_t)r * p.max_records + s_nrec[r]] = s_T[r];
-                    p.hDt[(int64_t)r * p.max_records + s_nrec[r]] = Dt;
+        // the step is accepted: history record, time, and the buffers swap
+        {
+            int rec = 0;
+            for (int r = 0; r < R; ++r) {
+                const int64_t gstep = s_step[r] + 1;
+                rec |= (p.record_step > 0 && gstep % p.record_step == 0 && s_nrec[r] < p.max_records);
+            }
+            if (rec) {
+                const StateView nxt = state_view(p, par ^ 1);
+                for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+                    const int r = (int)(q / N);
+                    const int64_t i = q - (int64_t)r * N;
+                    const int64_t gstep = s_step[r] + 1;
+                    if (p.record_step > 0 && gstep % p.record_step == 0 && s_nrec[r] < p.max_records) {
+                        const int64_t o = ((int64_t)r * p.max_records + s_nrec[r]) * N + i;
+                        p.hV[o] = nxt.V[q]; p.hD[o] = nxt.D[q]; p.hth[o] = nxt.theta[q]; p.hs[o] = nxt.sig_old[q];
+                        if (i == 0) {
+                            p.hT[(int64_t)r * p.max_records + s_nrec[r]] = s_T[r];
+                            p.hDt[(int64_t)r * p.max_records + s_nrec[r]] = s_dt[r];
+                        }
+                    }
                 }
             }
-            p.accel[q] = (p.Vn[q] - p.V[q]) / Dt;
-            p.D[q] = p.Dn[q];
-            if constexpr (!HM) {
-                reinterpret_cast<X*>(p.xd)[i * R + r] = (X)p.Dn[q];
-                fence_proxy_async_global();
-            }
-            p.theta[q] = p.thn[q];
-            p.V[q] = p.Vn[q];
-            p.fric[q] = p.fn[q];
-            p.sig_old[q] = p.sn[q];
         }
         __syncthreads();
         if (threadIdx.x < R) {
@@ -1064,16 +1181,29 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 s_nrec[r]++;
             s_T[r] = s_T[r] + s_dt[r];
             s_step[r] = gstep;
+            s_dta[r] = s_dt[r];
+            s_dt[r] = s_dtn[r];
         }
+        if (threadIdx.x == 0) s_par = par ^ 1;
         __syncthreads();
         lap(3);
         n_steps++;
+    }
+    // the state back into the host-visible buffers when it ended in the others
+    if (s_par) {
+        const StateView a = state_view(p, 0), b = state_view(p, 1);
+        for (int64_t q = gtid; q < (int64_t)R * N; q += nthreads) {
+            a.V[q] = b.V[q]; a.D[q] = b.D[q]; a.theta[q] = b.theta[q];
+            a.fric[q] = b.fric[q]; a.accel[q] = b.accel[q]; a.sig_old[q] = b.sig_old[q];
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.prof) {
         for (int k = 0; k < 4; ++k) atomicAdd(p.prof + k, s_tm[k]);
         atomicAdd(p.prof + 4, n_iter);
         atomicAdd(p.prof + 5, n_steps);
         for (int k = 0; k < 6; ++k) atomicAdd(p.prof + 10 + k, s_tm[4 + k]);
+        atomicAdd(p.prof + 16, s_tm[12]);
+        atomicAdd(p.prof + 17, s_tm[13]);
     }
     if (p.prof) {   // solver work of every thread, one atomic per warp and counter
         unsigned long long w[4] = {n_lo, it_lo, n_hi, it_hi};   // widened before the sums
@@ -1086,7 +1216,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     if (blockIdx.x == 0 && threadIdx.x < R) {
         const int r = threadIdx.x;
         p.T[r] = s_T[r];
-        p.dt[r] = s_dt[r];
+        p.dt[r] = s_dta[r];
         p.step[r] = s_step[r];
         p.nrec[r] = s_nrec[r];
         p.status[r] = s_fail[r];
@@ -1112,8 +1242,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
     pipe_init(pipe, smem_raw);
     X* xs = reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes);
     const int warp = threadIdx.x >> 5;
-    if (warp < kOpWarps) dense_matvec<M, R>(p, pipe, xs);          // the operator role
-    else if (threadIdx.x == kProducerWarp * 32) produce_tiles<M, R>(p, pipe, xs);
+    if (warp < kOpWarps) dense_matvec<M, R>(p, pipe, xs, 0);          // the operator role
+    else if (threadIdx.x == kProducerWarp * 32) produce_tiles<M, R>(p, pipe, xs, 0, reinterpret_cast<const X*>(p.xd));
 }
 
 template <class X, int R>
@@ -1211,7 +1341,8 @@ struct qdfn_ctx {
     unsigned char* unstable;
     int* has_unstable;
     double *V, *D, *theta, *fric, *accel, *sig_old, *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
-    int *instab, *flag, *sw;
+    int *instab, *flag, *sw, *sw_n;
+    double* accel_n;
     double *part_s = nullptr, *part_n = nullptr;
     double *T, *dt;
     int64_t *step, *nrec;
@@ -1231,8 +1362,9 @@ struct qdfn_ctx {
     double *ext_t = nullptr, *ext_n = nullptr, *ext_s = nullptr, *ext_p = nullptr;
     int nblocks = 0, nblocks_override = 0, nchunk = 1, nchunk2 = 1;
     int64_t chunk_len = 0, chunk_len2 = 0, rb_small0 = 0;
-    void* xd = nullptr;              // x copy of D (dense)
+    void* xd = nullptr;              // x copies of D (dense), two
     int64_t xbuf = 0;                // elements per shared-memory x buffer
+    int64_t xd_stride = 0, rb_stride = 0;
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1283,11 +1415,12 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.unstable = c->unstable; p.has_unstable = c->has_unstable;
     p.n_ext = c->n_ext; p.ext_t = c->ext_t; p.ext_n = c->ext_n; p.ext_s = c->ext_s; p.ext_p = c->ext_p;
     p.E = c->E; p.Kn = c->Kn; p.nchunk = c->nchunk; p.chunk_len = c->chunk_len;
-    p.xd = c->xd; p.xbuf = c->xbuf;
+    p.xd = c->xd; p.xbuf = c->xbuf; p.xd_stride = c->xd_stride; p.rb_stride = c->rb_stride;
     p.nchunk2 = c->nchunk2; p.chunk_len2 = c->chunk_len2; p.rb_small0 = c->rb_small0;
     p.V = c->V; p.D = c->D; p.theta = c->theta; p.fric = c->fric; p.accel = c->accel; p.sig_old = c->sig_old;
     p.Vn = c->Vn; p.Dn = c->Dn; p.thn = c->thn; p.fn = c->fn; p.sn = c->sn; p.dtall = c->dtall;
     p.tld = c->tld; p.knd = c->knd; p.instab = c->instab; p.flag = c->flag; p.sw = c->sw;
+    p.sw_n = c->sw_n; p.accel_n = c->accel_n;
     p.part_s = c->part_s; p.part_n = c->part_n;
     p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
@@ -1409,7 +1542,8 @@ int configure_launch(qdfn_ctx* c) {
         c->release(c->xd);
         c->xd = nullptr;
         // x copy of D: N columns padded to a multiple of 8 (+8), read in runs of 4
-        if ((rc = c->dalloc(reinterpret_cast<unsigned char**>(&c->xd), ((size_t)c->N + 16) * Rk * xsz))) return rc;
+        c->xd_stride = ((int64_t)c->N + 16) * Rk;   // elements per x copy (two: current and next step)
+        if ((rc = c->dalloc(reinterpret_cast<unsigned char**>(&c->xd), 2 * (size_t)c->xd_stride * xsz))) return rc;
         const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
         if ((rc = c->dalloc(&c->part_s, slots * Rk * c->N))) return rc;
         if ((rc = c->dalloc(&c->part_n, slots * Rk * c->N))) return rc;
@@ -1443,12 +1577,14 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
     A(V, RN); A(D, RN); A(theta, RN); A(fric, RN); A(accel, RN); A(sig_old, RN);
     A(Vn, RN); A(Dn, RN); A(thn, RN); A(fn, RN); A(sn, RN); A(dtall, RN); A(tld, RN); A(knd, RN);
-    A(instab, RN); A(flag, RN); A(sw, RN);
+    A(instab, RN); A(flag, RN); A(sw, RN); A(sw_n, RN); A(accel_n, RN);
     A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
-    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, kCounters); A(tile_ctr, 1);
-    A(solve_ctr, 1); A(tmax, 4); A(rb_done, (size_t)(N + kOpThreads - 1) / kOpThreads);   // row blocks of >= kOpThreads rows
+    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, kCounters); A(tile_ctr, 2);
+    // per-step counters, two sets used by alternate steps (one is reset while the other runs)
+    c->rb_stride = (N + kOpThreads - 1) / kOpThreads;   // row blocks have >= kOpThreads rows
+    A(solve_ctr, 2); A(tmax, 8); A(rb_done, 2 * (size_t)c->rb_stride);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0

@@ -182,8 +182,20 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
 
 // Implicit trapezoidal update with a secant iteration on V and the friction
 // inversion V = V0 exp((mu - mu0 - b ln(V0 theta/Dc))/a), all in FP64.
-__device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
-                               double SwitchV, int& err) {
+//
+// kPair: the solve of one patch runs on a lane pair (lanes 2k, 2k+1 of the
+// warp, same inputs).  The two evaluations of the secant step -- at V and at
+// V + DV -- are independent, so lane 2k evaluates at V and lane 2k+1 at V + DV,
+// and they exchange the residuals; everything else runs on both lanes alike.
+// The arithmetic and every branch decision are those of the one-lane solve
+// (an evaluation's error counts only when the one before it passed, as in the
+// sequential order), so both return the same result.  A lone warp issues one
+// FP64 instruction per ~70 cycles on this part, so halving the dependent chain
+// of an iteration matters where few warps are left to run (the last row
+// blocks of a step).
+template <bool kPair>
+__device__ PatchOut solve_lowv_t(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+                                 double SwitchV, int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;
     double V = p.VOld, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
@@ -201,26 +213,55 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
     } while (0)
 #define QDFN_FRICTION(Vx, Dx, Ax) \
     (inv_sig * (p.K_Self * (p.TLD - (Dx)) + p.tau0 - eta * (Vx) + p.dtau - p.Mass * (Ax)))
+    const int lane = threadIdx.x & 31, base = lane & ~1;
+    const unsigned pmask = 3u << base;
+    (void)lane; (void)pmask;
     while (maxDiff > crit) {
         Iteration++;
         const double VTest = V;
         const double DV = div_by(VTest, R1e10);
-        double Accel = div_by(V - p.VOld, Rdt);
-        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
-        if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
-        Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
-        Friction = QDFN_FRICTION(V, Disp, Accel);
-        double Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
-        const double FV = VTest - Vel;
-        V = V + DV;
-        const double VTest2 = V;
-        Accel = div_by(V - p.VOld, Rdt);
-        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
-        if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
-        Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
-        Friction = QDFN_FRICTION(V, Disp, Accel);
-        Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
-        const double FV_DeV = VTest2 - Vel;
+        double FV, FV_DeV, VTest2, Accel;
+        if constexpr (!kPair) {
+            Accel = div_by(V - p.VOld, Rdt);
+            Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
+            if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
+            Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
+            Friction = QDFN_FRICTION(V, Disp, Accel);
+            double Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
+            FV = VTest - Vel;
+            V = V + DV;
+            VTest2 = V;
+            Accel = div_by(V - p.VOld, Rdt);
+            Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
+            if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
+            Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
+            Friction = QDFN_FRICTION(V, Disp, Accel);
+            Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
+            FV_DeV = VTest2 - Vel;
+        } else {
+            // this lane's evaluation point: V (even lane) or V + DV (odd lane)
+            const double Vh = (lane & 1) ? VTest + DV : VTest;
+            int errh = 0;
+            const double Ah = div_by(Vh - p.VOld, Rdt);
+            const double Th = evolution(p.ThetaOld, Dt, Vh, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, errh);
+            const int failh = (Th < 0 || isnan(Th)) ? 1 : 0;
+            double FVh = 0;
+            if (!failh) {
+                const double Dh = p.DispOld + (p.VOld + Vh) / 2 * Dt;
+                const double Frh = QDFN_FRICTION(Vh, Dh, Ah);
+                const double Velh = kV0 * exp(div_by(Frh - p.Friction0 - p.b * jlog(div_by(kV0 * Th, Rdc), errh), Ra));
+                FVh = Vh - Velh;
+            }
+            const int fail0 = __shfl_sync(pmask, failh, base), fail1 = __shfl_sync(pmask, failh, base + 1);
+            const int err0 = __shfl_sync(pmask, errh, base), err1 = __shfl_sync(pmask, errh, base + 1);
+            FV = __shfl_sync(pmask, FVh, base);
+            FV_DeV = __shfl_sync(pmask, FVh, base + 1);
+            if (err0) err = err0;
+            if (fail0) { QDFN_FAIL_A(); break; }
+            if (err1) err = err1;        // the second evaluation runs only after the first passed
+            if (fail1) { QDFN_FAIL_A(); break; }
+            VTest2 = VTest + DV;
+        }
         V = VTest - FV * DV / (FV_DeV - FV);
         if (dr != 1 && V < 0)
             V = exp(jlog(VTest, err) - FV * jlog(VTest2 / VTest, err) / (FV_DeV - FV));
@@ -255,6 +296,10 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
     o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
     o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
     return o;
+}
+__device__ __forceinline__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+                                               double SwitchV, int& err) {
+    return solve_lowv_t<false>(p, Dt, eta, alpha, dr, SwitchV, err);
 }
 
 // InterpolateFromStressChange for one patch column.

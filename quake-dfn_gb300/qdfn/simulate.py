@@ -122,12 +122,13 @@ class Simulation:
         """Cumulative device counters: ns in time control / operator / solves /
         rotation, solve passes, steps, low-/high-velocity patch solves and their
         secant iterations."""
-        out = np.zeros(16, dtype=np.int64)
-        _lib.check(self.L.qdfn_get_counters(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)), 16))
+        out = np.zeros(18, dtype=np.int64)
+        _lib.check(self.L.qdfn_get_counters(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)), 18))
         keys = ("ns_control", "ns_operator", "ns_solve", "ns_rotate", "solve_passes", "steps",
                 "lowv_solves", "lowv_iterations", "highv_solves", "highv_iterations",
                 "ns_solve_own", "ns_solve_wait", "ns_operator_warps", "ns_solver_warps",
-                "ns_operator_warps_slowest", "ns_solver_warps_slowest")
+                "ns_operator_warps_slowest", "ns_solver_warps_slowest",
+                "ns_chunk_solve_longest", "ns_chunk_partials_longest")
         return {k: int(out[i]) for i, k in enumerate(keys)}
 
     # -- state --------------------------------------------------------------
