@@ -311,34 +311,30 @@ def run_ours(args):
     del Ks, Kn
     torch.cuda.empty_cache()
 
-    # ---- e2e through the C ABI with host buffers, same window
+    # ---- e2e through the C ABI with host buffers, same window: every step the
+    # whole ensemble state goes up from pinned host memory, one step runs, the
+    # state comes back (qdfn_set_state_all -> qdfn_run_async -> qdfn_get_state_all,
+    # one synchronisation per step)
     e2e = None
     if not args.no_e2e:
-        L = _lib.load()
         for r in range(R):
             sim.set_state(r, start_states[r])
-        pin = {k: [torch.empty(N, dtype=torch.float64).pin_memory() for _ in range(R)]
-               for k in ("V", "D", "theta", "friction", "accel", "sigma_old")}
-        for r in range(R):
-            for k in pin:
-                pin[k][r].copy_(torch.from_numpy(np.ascontiguousarray(start_states[r][k])))
-        Ts = [C.c_double(start_states[r]["T"]) for r in range(R)]
-        dts = [C.c_double(start_states[r]["dt"]) for r in range(R)]
-        steps = [C.c_int64(start_states[r]["step"]) for r in range(R)]
-        P = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
-        names = ("V", "D", "theta", "friction", "accel", "sigma_old")
+        names = simulate.Simulation.STATE_FIELDS
+        pin = {k: torch.empty((R, N), dtype=torch.float64).pin_memory() for k in names}
+        for k in names:
+            pin[k].copy_(torch.from_numpy(np.stack([np.ascontiguousarray(start_states[r][k]) for r in range(R)])))
+        Tp = torch.tensor([start_states[r]["T"] for r in range(R)], dtype=torch.float64).pin_memory()
+        dtp = torch.tensor([start_states[r]["dt"] for r in range(R)], dtype=torch.float64).pin_memory()
+        stp = torch.tensor([start_states[r]["step"] for r in range(R)], dtype=torch.int64).pin_memory()
+        sptr = stream.cuda_stream
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            for r in range(R):
-                _lib.check(L.qdfn_set_state(sim._h, r, *(P(pin[k][r]) for k in names), Ts[r].value, dts[r].value,
-                                            steps[r].value))
-            _lib.check(L.qdfn_run(sim._h, 1, TIMEOUT))
-            for r in range(R):
-                _lib.check(L.qdfn_get_state(sim._h, r, *(P(pin[k][r]) for k in names), C.byref(Ts[r]),
-                                            C.byref(dts[r]), C.byref(steps[r])))
+            sim.set_state_all(pin, Tp, dtp, stp, stream=sptr)
+            sim.run_async(1, stream=sptr, timeout_s=TIMEOUT)
+            sim.get_state_all(pin, Tp, dtp, stp, stream=sptr, wait=True)
         t_e2e = time.perf_counter() - t0
-        yrs = sum(Ts[r].value - start_states[r]["T"] for r in range(R)) / YEAR
+        yrs = float(sum(Tp[r].item() - start_states[r]["T"] for r in range(R))) / YEAR
         per_inst = 6 * N * 8 + 3 * 8
         e2e = {"value": (yrs * max(ws, 1)) / (t_e2e / 3600.0), "unit": "sim-years/hour",
                "h2d_bytes_per_step": R * per_inst, "d2h_bytes_per_step": R * per_inst}

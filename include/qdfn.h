@@ -200,6 +200,22 @@ int qdfn_set_state(qdfn_ctx* ctx, int inst, const double* V, const double* D,
                    const double* theta, const double* friction, const double* accel,
                    const double* sigma_old, double T, double dt, int64_t step);
 
+/* The state of every instance at once: host arrays [n_inst][N] (instance
+ * major), scalars [n_inst]; any pointer may be NULL.  The copies are enqueued
+ * on `stream` (a cudaStream_t as void*, NULL = default stream); from pinned
+ * host memory they do not block the caller.  qdfn_get_state_all with wait = 1
+ * synchronises the stream, and when the context's run is in flight on that
+ * stream it completes the run like qdfn_sync (same status codes), so a host
+ * loop set_state_all -> run_async -> get_state_all costs one synchronisation.
+ * No counterpart in the reference (its state stays inside the Julia process);
+ * they serve callers that keep the ensemble state on the host between steps. */
+int qdfn_set_state_all(qdfn_ctx* ctx, const double* V, const double* D, const double* theta,
+                       const double* friction, const double* accel, const double* sigma_old,
+                       const double* T, const double* dt, const int64_t* step, void* stream);
+int qdfn_get_state_all(qdfn_ctx* ctx, double* V, double* D, double* theta, double* friction,
+                       double* accel, double* sigma_old, double* T, double* dt, int64_t* step,
+                       void* stream, int wait);
+
 /* History of one instance: records 0..*nrec-1 (History_Time, History_Dt and the
  * record x N arrays History_V/_Disp/_Theta/_NormalStress).  Any pointer may be
  * NULL; nrec receives the number of records written so far. */

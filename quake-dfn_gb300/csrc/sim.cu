@@ -1369,6 +1369,7 @@ struct qdfn_ctx {
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
     cudaStream_t pending = nullptr;
+    int* host_status = nullptr;      // pinned: [0] error flag, [1..] instance status (run completion)
     bool running = false;
 
     template <class T>
@@ -1388,6 +1389,7 @@ struct qdfn_ctx {
     }
     ~qdfn_ctx() {
         for (void* q : allocs) cudaFree(q);
+        if (host_status) cudaFreeHost(host_status);
     }
 };
 
@@ -1542,8 +1544,13 @@ int configure_launch(qdfn_ctx* c) {
         c->release(c->xd);
         c->xd = nullptr;
         // x copy of D: N columns padded to a multiple of 8 (+8), read in runs of 4
-        c->xd_stride = ((int64_t)c->N + 16) * Rk;   // elements per x copy (two: current and next step)
+        // elements per x copy (two: current and next step), a multiple of 32 so
+        // that the second copy starts 16-byte aligned like the first (bulk copies
+        // need 16-byte aligned sources)
+        c->xd_stride = (((int64_t)c->N + 16) * Rk + 31) / 32 * 32;
         if ((rc = c->dalloc(reinterpret_cast<unsigned char**>(&c->xd), 2 * (size_t)c->xd_stride * xsz))) return rc;
+        if ((reinterpret_cast<uintptr_t>(c->xd) | (uintptr_t)(c->xd_stride * xsz)) % 16 != 0)
+            return fail(QDFN_ERR_INVALID, "x copy of D not 16-byte aligned");
         const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
         if ((rc = c->dalloc(&c->part_s, slots * Rk * c->N))) return rc;
         if ((rc = c->dalloc(&c->part_n, slots * Rk * c->N))) return rc;
@@ -1828,6 +1835,60 @@ extern "C" int qdfn_set_state(qdfn_ctx* c, int inst, const double* V, const doub
     QDFN_CUDA(cudaMemcpy(c->T + inst, &T, 8, cudaMemcpyHostToDevice));
     QDFN_CUDA(cudaMemcpy(c->dt + inst, &dt, 8, cudaMemcpyHostToDevice));
     QDFN_CUDA(cudaMemcpy(c->step + inst, &step, 8, cudaMemcpyHostToDevice));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_set_state_all(qdfn_ctx* c, const double* V, const double* D, const double* theta,
+                                  const double* friction, const double* accel, const double* sigma_old,
+                                  const double* T, const double* dt, const int64_t* step, void* stream) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (c->running) return fail(QDFN_ERR_STATE, "a run is in flight (qdfn_sync or qdfn_get_state_all first)");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)c->R * c->N * 8, ns = (size_t)c->R * 8;
+    if (V) QDFN_CUDA(cudaMemcpyAsync(c->V, V, n, cudaMemcpyHostToDevice, st));
+    if (D) QDFN_CUDA(cudaMemcpyAsync(c->D, D, n, cudaMemcpyHostToDevice, st));
+    if (theta) QDFN_CUDA(cudaMemcpyAsync(c->theta, theta, n, cudaMemcpyHostToDevice, st));
+    if (friction) QDFN_CUDA(cudaMemcpyAsync(c->fric, friction, n, cudaMemcpyHostToDevice, st));
+    if (accel) QDFN_CUDA(cudaMemcpyAsync(c->accel, accel, n, cudaMemcpyHostToDevice, st));
+    if (sigma_old) QDFN_CUDA(cudaMemcpyAsync(c->sig_old, sigma_old, n, cudaMemcpyHostToDevice, st));
+    if (T) QDFN_CUDA(cudaMemcpyAsync(c->T, T, ns, cudaMemcpyHostToDevice, st));
+    if (dt) QDFN_CUDA(cudaMemcpyAsync(c->dt, dt, ns, cudaMemcpyHostToDevice, st));
+    if (step) QDFN_CUDA(cudaMemcpyAsync(c->step, step, ns, cudaMemcpyHostToDevice, st));
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_get_state_all(qdfn_ctx* c, double* V, double* D, double* theta, double* friction,
+                                  double* accel, double* sigma_old, double* T, double* dt, int64_t* step,
+                                  void* stream, int wait) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool completes = c->running && c->pending == st;
+    if (c->running && !completes) return fail(QDFN_ERR_STATE, "the run in flight is on another stream");
+    if (completes && !wait) return fail(QDFN_ERR_INVALID, "reading the state of a run in flight needs wait=1");
+    const size_t n = (size_t)c->R * c->N * 8, ns = (size_t)c->R * 8;
+    if (V) QDFN_CUDA(cudaMemcpyAsync(V, c->V, n, cudaMemcpyDeviceToHost, st));
+    if (D) QDFN_CUDA(cudaMemcpyAsync(D, c->D, n, cudaMemcpyDeviceToHost, st));
+    if (theta) QDFN_CUDA(cudaMemcpyAsync(theta, c->theta, n, cudaMemcpyDeviceToHost, st));
+    if (friction) QDFN_CUDA(cudaMemcpyAsync(friction, c->fric, n, cudaMemcpyDeviceToHost, st));
+    if (accel) QDFN_CUDA(cudaMemcpyAsync(accel, c->accel, n, cudaMemcpyDeviceToHost, st));
+    if (sigma_old) QDFN_CUDA(cudaMemcpyAsync(sigma_old, c->sig_old, n, cudaMemcpyDeviceToHost, st));
+    if (T) QDFN_CUDA(cudaMemcpyAsync(T, c->T, ns, cudaMemcpyDeviceToHost, st));
+    if (dt) QDFN_CUDA(cudaMemcpyAsync(dt, c->dt, ns, cudaMemcpyDeviceToHost, st));
+    if (step) QDFN_CUDA(cudaMemcpyAsync(step, c->step, ns, cudaMemcpyDeviceToHost, st));
+    if (completes) {   // the run's outcome travels with the state: one synchronisation
+        if (!c->host_status) QDFN_CUDA(cudaHostAlloc(&c->host_status, (1 + kMaxInst) * sizeof(int), 0));
+        QDFN_CUDA(cudaMemcpyAsync(c->host_status, c->gerr, sizeof(int), cudaMemcpyDeviceToHost, st));
+        QDFN_CUDA(cudaMemcpyAsync(c->host_status + 1, c->status, c->R * sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    if (!wait) return QDFN_OK;
+    QDFN_CUDA(cudaStreamSynchronize(st));
+    if (completes) {
+        c->running = false;
+        for (int r = 0; r < c->R; ++r)
+            if (c->host_status[1 + r] != 0)
+                return fail(c->host_status[1 + r], "instance " + std::to_string(r) + " stopped");
+        if (c->host_status[0] != 0) return fail(c->host_status[0], "device loop stopped early");
+    }
     return QDFN_OK;
 }
 

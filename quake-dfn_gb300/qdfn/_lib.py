@@ -30,7 +30,7 @@ EXPORTS = [
     "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
     "qdfn_get_counters",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
-    "qdfn_apply_dense_noalloc",
+    "qdfn_apply_dense_noalloc", "qdfn_set_state_all", "qdfn_get_state_all",
 ]
 
 
@@ -93,6 +93,9 @@ def load():
     L.qdfn_get_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 8 + [_ip]
     L.qdfn_set_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [C.c_double, C.c_double, C.c_int64]
     L.qdfn_get_history.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [_ip]
+    # whole-ensemble state: raw addresses, so that pinned tensors pass straight through
+    L.qdfn_set_state_all.argtypes = [C.c_void_p] + [C.c_void_p] * 9 + [C.c_void_p]
+    L.qdfn_get_state_all.argtypes = [C.c_void_p] + [C.c_void_p] * 9 + [C.c_void_p, C.c_int]
     L.qdfn_apply_operator.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.qdfn_get_kself.argtypes = [C.c_void_p, _dp]
     L.qdfn_apply_dense_noalloc.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,

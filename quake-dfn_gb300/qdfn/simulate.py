@@ -22,6 +22,17 @@ def _f64(a, n=None):
     return a
 
 
+def _addr(buf):
+    """Address of a host buffer: numpy array or an object with data_ptr()."""
+    if buf is None:
+        return None
+    if hasattr(buf, "data_ptr"):
+        return C.c_void_p(buf.data_ptr())
+    if not (buf.flags.c_contiguous and buf.flags.writeable):
+        raise ValueError("host buffers must be C-contiguous and writeable")
+    return C.c_void_p(buf.ctypes.data)
+
+
 class Simulation:
     """One qdfn context: ``n_inst`` instances (friction draws) sharing an operator.
 
@@ -146,6 +157,24 @@ class Simulation:
         arrs = [_f64(st[k], self.N) for k in ("V", "D", "theta", "friction", "accel", "sigma_old")]
         _lib.check(self.L.qdfn_set_state(self._h, inst, *(_lib.dp(a) for a in arrs), float(st["T"]),
                                          float(st["dt"]), int(st["step"])))
+
+    STATE_FIELDS = ("V", "D", "theta", "friction", "accel", "sigma_old")
+
+    def set_state_all(self, arrays, T, dt, step, stream=0):
+        """Enqueue the state of every instance: arrays maps each STATE_FIELDS
+        name to a host buffer of n_inst*N float64 (numpy array, or any object
+        with a data_ptr(), e.g. a pinned CPU tensor); T, dt, step: n_inst
+        values (float64, float64, int64 buffers).  Asynchronous on `stream`."""
+        ptrs = [_addr(arrays[k]) if k in arrays else None for k in self.STATE_FIELDS]
+        _lib.check(self.L.qdfn_set_state_all(self._h, *ptrs, _addr(T), _addr(dt), _addr(step), C.c_void_p(stream)))
+
+    def get_state_all(self, arrays, T, dt, step, stream=0, wait=True):
+        """Enqueue the copy of every instance's state into host buffers (as in
+        set_state_all); wait=True synchronises and completes a run in flight on
+        `stream` (raising its error like sync())."""
+        ptrs = [_addr(arrays[k]) if k in arrays else None for k in self.STATE_FIELDS]
+        _lib.check(self.L.qdfn_get_state_all(self._h, *ptrs, _addr(T), _addr(dt), _addr(step),
+                                             C.c_void_p(stream), 1 if wait else 0))
 
     def history(self, inst=0):
         n = C.c_int64()

@@ -123,6 +123,76 @@ def test_instances_match_independent_oracle_runs(qdfn_mod, oracle_mod, n_inst):
         assert _rel(st["D"], o.state["D"]) < 1e-9
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("n_inst", [1, 3])
+def test_odd_sized_system_tracks_the_oracle(qdfn_mod, oracle_mod, precision, n_inst):
+    """N = 49 (odd) with 1 and 3 instances: the step loop's second state
+    buffer and the operator's second copy of D start at an odd element offset
+    unless padded, which bulk copies cannot read.  FP32 runs the overlapped
+    operator/solve phase (lane-pair solves); FP64 the sequential one.  Both
+    follow the FP64 oracle: FP64 to rounding, FP32 within its operator error."""
+    from qdfn import synth
+    rec = small_network(seed=1)["records"]
+    assert rec.shape[0] % 2 == 1
+    Ks, Kn, prob, ext, oprob = _setup(oracle_mod, rec)
+    N = rec.shape[0]
+    draws = synth.friction_draws(dict(prob, N=N), n_inst, seed=9)
+    mprob = dict(prob)
+    for k in ("a", "b", "Dc", "theta_i", "V_i", "f_i"):
+        mprob[k] = draws[k]
+    sim = _gpu_sim(mprob, Ks, Kn, ext, precision=precision, n_inst=n_inst)
+    nsteps, tol = (101, 1e-9) if precision == "fp64" else (41, 1e-4)
+    sim.run(nsteps, timeout_s=120)
+    for r in range(n_inst):
+        op = dict(oprob)
+        for k in ("a", "b", "Dc", "theta_i", "V_i", "f_i"):
+            op[k] = draws[k][r * N:(r + 1) * N]
+        o = oracle_mod.Simulation(op, ("dense", Ks, Kn))
+        o.run(nsteps)
+        st = sim.state(r)
+        assert st["step"] == o.step == nsteps
+        assert abs(st["T"] / o.T - 1) < tol
+        assert _rel(st["D"], o.state["D"]) < tol
+        assert _rel(st["V"], o.state["V"]) < tol
+
+
+def test_ensemble_state_transfer_matches_per_instance_api(qdfn_mod, oracle_mod):
+    """qdfn_get_state_all / qdfn_set_state_all move the same bytes as the
+    per-instance calls, and set_state_all -> run_async -> get_state_all (one
+    synchronisation) continues a run exactly like set_state -> run -> state."""
+    from qdfn import synth
+    rec = small_network()["records"]
+    Ks, Kn, prob, ext, _ = _setup(oracle_mod, rec)
+    N, R = rec.shape[0], 3
+    draws = synth.friction_draws(dict(prob, N=N), R, seed=4)
+    mprob = dict(prob)
+    for k in ("a", "b", "Dc", "theta_i", "V_i", "f_i"):
+        mprob[k] = draws[k]
+    a = _gpu_sim(mprob, Ks, Kn, ext, n_inst=R)
+    a.run(30)
+    names = a.STATE_FIELDS
+    arr = {k: np.full(R * N, np.nan) for k in names}
+    T, dt, step = np.zeros(R), np.zeros(R), np.zeros(R, dtype=np.int64)
+    a.get_state_all(arr, T, dt, step)
+    for r in range(R):
+        st = a.state(r)
+        for k in names:
+            assert np.array_equal(arr[k][r * N:(r + 1) * N], st[k])
+        assert T[r] == st["T"] and dt[r] == st["dt"] and step[r] == st["step"]
+    b = _gpu_sim(mprob, Ks, Kn, ext, n_inst=R)
+    b.set_state_all(arr, T, dt, step)
+    b.run_async(12)
+    out = {k: np.zeros(R * N) for k in names}
+    T2, dt2, step2 = np.zeros(R), np.zeros(R), np.zeros(R, dtype=np.int64)
+    b.get_state_all(out, T2, dt2, step2, wait=True)
+    a.run(12)
+    for r in range(R):
+        st = a.state(r)
+        for k in names:
+            assert np.array_equal(out[k][r * N:(r + 1) * N], st[k])
+        assert T2[r] == st["T"] and step2[r] == st["step"] == 42
+
+
 def test_state_roundtrip_resumes_identically(qdfn_mod, oracle_mod):
     rec = mixed_rects()
     Ks, Kn, prob, ext, _ = _setup(oracle_mod, rec)
