@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="network", choices=["network", "ensemble"],
+                    help="network: the 30-fault network (default); ensemble: 64 geometries of "
+                         "800-6,000 patches x 4 friction draws advanced together")
+    ap.add_argument("--geometries", type=int, default=64)
     return ap.parse_args()
 
 
@@ -486,10 +490,79 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def ensemble_geometries(n_geo, seed=11):
+    """Geometries drawn as the network (strike, dip, lengths, depths, friction)
+    with 3-40 faults each; the patch size is set per geometry so that it holds
+    800-6,000 patches (drawn log-uniformly)."""
+    from qdfn import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(n_geo):
+        nf = int(rng.integers(3, 41))
+        target = float(np.exp(rng.uniform(np.log(800), np.log(6000))))
+        probe = synth.fault_network(seed=1000 + g, n_faults=nf, patch=200.0)
+        patch = 200.0 * np.sqrt(probe["N"] / target)
+        sysd = synth.fault_network(seed=1000 + g, n_faults=nf, patch=float(patch))
+        out.append(sysd)
+    return out
+
+
+def run_ensemble(args):
+    """Batched ensemble: every geometry with its friction draws is one
+    context on a share of the SMs, all advanced together (qdfn.ensemble)."""
+    import torch
+    from qdfn import assemble, ensemble, synth
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    geos = ensemble_geometries(args.geometries)
+    members = []
+    for g, sysd in enumerate(geos):
+        N = sysd["N"]
+        rec = torch.tensor(sysd["records"], dtype=torch.float64, device=dev)
+        Ks = torch.empty((N, N), dtype=torch.float64, device=dev)
+        Kn = torch.empty((N, N), dtype=torch.float64, device=dev)
+        assemble.assemble_rect_dev(rec, rec, sysd["G"], sysd["nu"], Ks, Kn, layout="col")
+        kdiag = torch.diagonal(Ks).cpu().numpy()
+        draws = synth.friction_draws(sysd, args.inst, seed=g + 1)
+        prob = synth.problem_dict(sysd, kdiag, n_inst=args.inst, draws=draws)
+        ext = synth.external_ramp(N, sysd["stressing_rate"], 1e12)
+        members.append(dict(problem=prob, n_inst=args.inst, Ks=Ks, Kn=Kn, ext=ext))
+    ens = ensemble.Ensemble(members, precision=args.precision)
+    del members
+    torch.cuda.empty_cache()
+    ens.run(args.warmup, timeout_s=TIMEOUT)
+    y0 = ens.sim_years()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    ens.run(args.steps, timeout_s=TIMEOUT)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    yrs = float(np.sum(ens.sim_years() - y0))
+    sizes = [m.N for m in ens.members]
+    line = {"metric": "ensemble sim-years/hour (batched geometries)", "value": yrs / (wall / 3600.0),
+            "unit": "sim-years/hour", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "%s-operator/fp64-state" % args.precision, "data": "synthetic",
+            "config": {"workload": "%d geometries of %d-%d patches (%d total) x %d friction draws, one context "
+                                   "per geometry on its share of the SMs, all advanced together"
+                                   % (len(sizes), min(sizes), max(sizes), sum(sizes), args.inst),
+                       "instances": len(sizes) * args.inst, "precision": args.precision,
+                       "sm_shares": [int(b) for b in ens.blocks]},
+            "gpu_launches": len(sizes), "clocks": clk,
+            "note": "wall clock over all members' concurrent launches (each member takes its own adaptive steps)"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
     else:
         run_ours(args)
 

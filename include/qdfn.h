@@ -177,6 +177,16 @@ int qdfn_sync(qdfn_ctx* ctx);
 
 /* Number of device kernels one qdfn_run launches (for launch accounting). */
 int qdfn_kernels_per_run(const qdfn_ctx* ctx);
+
+/* Cap the thread blocks (one per SM) a context's runs use; 0 = every SM
+ * (default).  Contexts whose caps add up to at most the SM count run side by
+ * side when launched with qdfn_run_async on different streams -- a batched
+ * ensemble of geometries of uneven size, each on its share of the GPU.  The
+ * operator tiling is re-sized for the cap.  qdfn_get_blocks returns the block
+ * count of the next run (-1 for a null context).  No counterpart in the
+ * reference, which runs one geometry per process. */
+int qdfn_set_blocks(qdfn_ctx* ctx, int nblocks);
+int qdfn_get_blocks(const qdfn_ctx* ctx);
 /* Cumulative device counters of the context's runs (first n of): ns spent in
  * [0] time-step control, [1] elastic operator, [2] friction solves and retries,
  * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps;

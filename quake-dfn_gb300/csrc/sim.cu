@@ -1481,8 +1481,11 @@ int configure_launch(qdfn_ctx* c) {
     const int Rk = kernel_R(c->R);
     const int vec = c->prec == QDFN_FP64 ? 1 : 2;
     const size_t xsz = c->prec == QDFN_FP64 ? 8 : 4;
-    const int sms = num_sms();
-    if (sms <= 0) return fail(QDFN_ERR_CUDA, "no CUDA device");
+    const int dev_sms = num_sms();
+    if (dev_sms <= 0) return fail(QDFN_ERR_CUDA, "no CUDA device");
+    // the SMs this context's runs may use (qdfn_set_blocks caps them so that
+    // several contexts run side by side); the tiling is sized for them
+    const int sms = c->nblocks_override > 0 ? std::min(dev_sms, c->nblocks_override) : dev_sms;
     SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
     int64_t want_blocks;
     if (c->hmat) {
@@ -1793,6 +1796,16 @@ extern "C" int qdfn_run(qdfn_ctx* c, int64_t nsteps, double timeout_s) {
 }
 
 extern "C" int qdfn_kernels_per_run(const qdfn_ctx* c) { return c ? 1 : 0; }
+
+extern "C" int qdfn_set_blocks(qdfn_ctx* c, int nblocks) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (nblocks < 0) return fail(QDFN_ERR_INVALID, "nblocks < 0");
+    if (c->running) return fail(QDFN_ERR_STATE, "a run is in flight");
+    c->nblocks_override = nblocks;
+    return c->prec < 0 ? QDFN_OK : configure_launch(c);
+}
+
+extern "C" int qdfn_get_blocks(const qdfn_ctx* c) { return c ? c->nblocks : -1; }
 
 extern "C" int qdfn_get_counters(const qdfn_ctx* c, int64_t* out, int n) {
     if (!c || !out || n < 0) return fail(QDFN_ERR_INVALID, "null argument");

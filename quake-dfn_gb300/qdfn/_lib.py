@@ -30,7 +30,8 @@ EXPORTS = [
     "qdfn_set_external_stress", "qdfn_run", "qdfn_run_async", "qdfn_sync", "qdfn_kernels_per_run",
     "qdfn_get_counters",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
-    "qdfn_apply_dense_noalloc", "qdfn_set_state_all", "qdfn_get_state_all",
+    "qdfn_apply_dense_noalloc", "qdfn_set_state_all", "qdfn_get_state_all", "qdfn_set_blocks",
+    "qdfn_get_blocks",
 ]
 
 
@@ -89,6 +90,8 @@ def load():
     L.qdfn_run_async.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
     L.qdfn_sync.argtypes = [C.c_void_p]
     L.qdfn_kernels_per_run.argtypes = [C.c_void_p]
+    L.qdfn_set_blocks.argtypes = [C.c_void_p, C.c_int]
+    L.qdfn_get_blocks.argtypes = [C.c_void_p]
     L.qdfn_get_counters.argtypes = [C.c_void_p, _ip, C.c_int]
     L.qdfn_get_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 8 + [_ip]
     L.qdfn_set_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [C.c_double, C.c_double, C.c_int64]

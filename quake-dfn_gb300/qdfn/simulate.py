@@ -129,6 +129,13 @@ class Simulation:
     def kernels_per_run(self):
         return self.L.qdfn_kernels_per_run(self._h)
 
+    def set_blocks(self, nblocks):
+        """Cap the SMs (thread blocks) this context's runs use (0 = all)."""
+        _lib.check(self.L.qdfn_set_blocks(self._h, int(nblocks)))
+
+    def blocks(self):
+        return self.L.qdfn_get_blocks(self._h)
+
     def counters(self):
         """Cumulative device counters: ns in time control / operator / solves /
         rotation, solve passes, steps, low-/high-velocity patch solves and their
