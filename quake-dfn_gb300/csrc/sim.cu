@@ -122,6 +122,7 @@ struct SimParams {
     uint64_t budget_ns;             // wall-time budget of this launch
     unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
     int64_t n_rb;                    // dense: operator row blocks
+    int hold_cap;                    // dense: row chunks a block may hold at once in the overlapped phase
     unsigned long long* tmax;        // [2][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, chunk partial sums), ns
 };
@@ -981,8 +982,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             // own operator products, so the result is the same as running the
             // phases one after the other.
             __shared__ int s_fused_fail;
+            __shared__ int s_held;       // row chunks this block holds (grabbed, not yet solved)
             __shared__ unsigned long long s_t_solve;
-            if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; }
+            if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; s_held = 0; }
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1006,10 +1008,36 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 const int64_t nk = p.n_rb * R * cpr;
                 const unsigned* rbd = p.rb_done + cpar * p.rb_stride;
                 for (;;) {
+                    // a block holds at most hold_cap chunks at a time, so that the
+                    // chunks of the last row blocks, which complete together at
+                    // the end of the stream, spread over the SMs
                     unsigned long long k = 0;
-                    if (lane == 0) k = atomicAdd(p.solve_ctr + cpar, 1ull);
+                    int okh = 1;
+                    if (lane == 0) {
+                        if (atomicAdd(&s_held, 1) >= p.hold_cap) {
+                            const uint64_t t0 = globaltimer_ns();
+                            do {
+                                atomicSub(&s_held, 1);
+                                if (globaltimer_ns() - t0 > kWaitLimitNs || *(volatile int*)p.gerr != 0) {
+                                    okh = 0;
+                                    break;
+                                }
+                                __nanosleep(128);
+                            } while (atomicAdd(&s_held, 1) >= p.hold_cap);
+                        }
+                        if (okh) k = atomicAdd(p.solve_ctr + cpar, 1ull);
+                    }
+                    okh = __shfl_sync(0xffffffffu, okh, 0);
+                    if (!okh) {
+                        if (lane == 0) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+                        s_fused_fail = 1;
+                        break;
+                    }
                     k = __shfl_sync(0xffffffffu, k, 0);
-                    if ((int64_t)k >= nk) break;
+                    if ((int64_t)k >= nk) {
+                        if (lane == 0) atomicSub(&s_held, 1);
+                        break;
+                    }
                     const int64_t rb = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
                     const int r = (int)(rem / cpr);
                     const int64_t i = rb * rpb + (rem % cpr) * 16 + (lane >> 1);
@@ -1029,13 +1057,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     }
                     ok = __shfl_sync(0xffffffffu, ok, 0);
                     if (!ok) {
-                        if (lane == 0) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+                        if (lane == 0) { atomicExch(p.gerr, QDFN_ERR_TIMEOUT); atomicSub(&s_held, 1); }
                         s_fused_fail = 1;
                         break;
                     }
                     const uint64_t t_ready = globaltimer_ns();
                     if (i < N) solve_item((int64_t)r * N + i, r, i, true, true);
+                    __syncwarp();
                     if (lane == 0) {
+                        atomicSub(&s_held, 1);
                         atomicMax(p.tmax + cpar * 4 + 2, (unsigned long long)(globaltimer_ns() - t_ready));
                         atomicMax(p.tmax + cpar * 4 + 3, (unsigned long long)t_sp);
                     }
@@ -1365,6 +1395,7 @@ struct qdfn_ctx {
     void* xd = nullptr;              // x copies of D (dense), two
     int64_t xbuf = 0;                // elements per shared-memory x buffer
     int64_t xd_stride = 0, rb_stride = 0;
+    int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1432,6 +1463,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.solve_ctr = c->solve_ctr;
     p.rb_done = c->rb_done;
     p.tmax = c->tmax;
+    p.hold_cap = c->hold_cap;
     p.n_rb = c->ld > 0 ? (c->N + c->ld - 1) / c->ld : 0;
     p.h = c->hops;
     p.budget_ns = budget_ns;
@@ -1501,6 +1533,7 @@ int configure_launch(qdfn_ctx* c) {
         // tiles per SM and step before the guided tail (tuning knob QDFN_TILES_PER_SM)
         int64_t tiles_per_sm = 3;
         if (const char* e = std::getenv("QDFN_TILES_PER_SM")) tiles_per_sm = std::max(1, std::min(64, std::atoi(e)));
+        if (const char* e = std::getenv("QDFN_SOLVE_HOLD")) c->hold_cap = std::max(1, std::min(64, std::atoi(e)));
         int64_t want_chunks = std::max<int64_t>(1, (tiles_per_sm * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
         // two x buffers (R x chunk x elem each) share the 227 KB with the 192 KB stage ring
