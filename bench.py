@@ -324,11 +324,14 @@ def run_ours(args):
         for r in range(R):
             sim.set_state(r, start_states[r])
         names = simulate.Simulation.STATE_FIELDS
-        pin = {k: torch.empty((R, N), dtype=torch.float64).pin_memory() for k in names}
+        # one pinned block [field][instance][patch]: the library moves it in one copy per direction
+        pin6 = torch.empty((len(names), R, N), dtype=torch.float64).pin_memory()
+        pin = {k: pin6[f] for f, k in enumerate(names)}
         for k in names:
             pin[k].copy_(torch.from_numpy(np.stack([np.ascontiguousarray(start_states[r][k]) for r in range(R)])))
-        Tp = torch.tensor([start_states[r]["T"] for r in range(R)], dtype=torch.float64).pin_memory()
-        dtp = torch.tensor([start_states[r]["dt"] for r in range(R)], dtype=torch.float64).pin_memory()
+        Tdt = torch.tensor([[start_states[r]["T"] for r in range(R)], [start_states[r]["dt"] for r in range(R)]],
+                           dtype=torch.float64).pin_memory()
+        Tp, dtp = Tdt[0], Tdt[1]
         stp = torch.tensor([start_states[r]["step"] for r in range(R)], dtype=torch.int64).pin_memory()
         sptr = stream.cuda_stream
         torch.cuda.synchronize()

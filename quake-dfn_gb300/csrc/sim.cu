@@ -1541,8 +1541,11 @@ int configure_launch(qdfn_ctx* c) {
         clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), std::min<int64_t>(2048, cmax)) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
-        // half-width tiles for the row blocks of the last two waves of tiles
-        c->chunk_len2 = std::max<int64_t>(8, ((clen + 1) / 2 + 7) / 8 * 8);
+        // narrower tiles (1/tail_div of the width; QDFN_TAIL_DIV, default 2) for
+        // the row blocks of the last two waves of tiles
+        int64_t tail_div = 2;
+        if (const char* e = std::getenv("QDFN_TAIL_DIV")) tail_div = std::max(1, std::min(16, std::atoi(e)));
+        c->chunk_len2 = std::max<int64_t>(8, ((clen + tail_div - 1) / tail_div + 7) / 8 * 8);
         c->nchunk2 = (int)((c->N + c->chunk_len2 - 1) / c->chunk_len2);
         const int64_t nsmall = std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
         c->rb_small0 = nrb - nsmall;
@@ -1618,13 +1621,32 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
 #define A(ptr, n) if (!rc) rc = c->dalloc(&c->ptr, n)
     A(a, RN); A(b, RN); A(Dc, RN); A(F0, RN); A(tau0, RN); A(sigma0, RN); A(Vconst, RN);
     A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
-    A(V, RN); A(D, RN); A(theta, RN); A(fric, RN); A(accel, RN); A(sig_old, RN);
+    // the six host-visible state fields in one block, in the order of the
+    // state-transfer calls, so that contiguous host buffers move in one copy
+    double* state6 = nullptr;
+    if (!rc) rc = c->dalloc(&state6, 6 * RN);
+    if (!rc) {
+        c->V = state6; c->D = state6 + RN; c->theta = state6 + 2 * RN;
+        c->fric = state6 + 3 * RN; c->accel = state6 + 4 * RN; c->sig_old = state6 + 5 * RN;
+    }
     A(Vn, RN); A(Dn, RN); A(thn, RN); A(fn, RN); A(sn, RN); A(dtall, RN); A(tld, RN); A(knd, RN);
     A(instab, RN); A(flag, RN); A(sw, RN); A(sw_n, RN); A(accel_n, RN);
-    A(T, (size_t)Rk); A(dt, (size_t)Rk); A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
+    double* Tdt = nullptr;           // T and dt side by side, for the same reason
+    if (!rc) rc = c->dalloc(&Tdt, 2 * (size_t)Rk);
+    if (!rc) { c->T = Tdt; c->dt = Tdt + Rk; }
+    A(step, (size_t)Rk); A(nrec, (size_t)Rk); A(status, (size_t)Rk);
     const size_t hr = (size_t)Rk * std::max<int64_t>(pr->max_records, 1);
     A(hT, hr); A(hDt, hr); A(hV, hr * N); A(hD, hr * N); A(hth, hr * N); A(hs, hr * N);
-    A(bar_count, 1); A(bar_gen, 1); A(gerr, 1); A(prof, kCounters); A(tile_ctr, 2);
+    // launch control words side by side: [0] error flag, [1] barrier arrivals,
+    // [2] barrier generation -- the first two are cleared by one memset per launch
+    int* ctrl = nullptr;
+    if (!rc) rc = c->dalloc(&ctrl, 4);
+    if (!rc) {
+        c->gerr = ctrl;
+        c->bar_count = reinterpret_cast<unsigned*>(ctrl + 1);
+        c->bar_gen = reinterpret_cast<unsigned*>(ctrl + 2);
+    }
+    A(prof, kCounters); A(tile_ctr, 2);
     // per-step counters, two sets used by alternate steps (one is reset while the other runs)
     c->rb_stride = (N + kOpThreads - 1) / kOpThreads;   // row blocks have >= kOpThreads rows
     A(solve_ctr, 2); A(tmax, 8); A(rb_done, 2 * (size_t)c->rb_stride);
@@ -1794,9 +1816,8 @@ extern "C" int qdfn_run_async(qdfn_ctx* c, int64_t nsteps, double timeout_s, voi
     const double budget = timeout_s > 0 ? timeout_s : 1e6;
     const uint64_t budget_ns = (uint64_t)(budget * 1e9);
     cudaStream_t st = (cudaStream_t)stream;
-    QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, sizeof(int), st));
-    QDFN_CUDA(cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), st));
-    QDFN_CUDA(cudaMemsetAsync(c->tile_ctr, 0, sizeof(unsigned long long), st));
+    // error flag and barrier arrivals (adjacent); the kernel resets its own counters
+    QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, 2 * sizeof(int), st));
     SimParams p = make_params(c, budget_ns);
     SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
     void* args[] = {&p, &nsteps};
@@ -1884,6 +1905,41 @@ extern "C" int qdfn_set_state(qdfn_ctx* c, int inst, const double* V, const doub
     return QDFN_OK;
 }
 
+namespace {
+// Field copies of a state transfer; a field whose device and host buffers both
+// follow the previous one's (device fields are `dstride` bytes apart, host
+// buffers are packed: the caller's arrays for consecutive fields end to end)
+// joins its copy, so packed host buffers move in one copy per direction.
+struct CopyList {
+    struct Run { char* dev; char* host; size_t bytes, dstride; int nf; };
+    Run runs[9];
+    int n = 0;
+    void add(void* dev, const void* host, size_t bytes, size_t dstride) {
+        if (!host) return;
+        char* d = (char*)dev;
+        char* h = (char*)const_cast<void*>(host);
+        if (n > 0) {
+            Run& r = runs[n - 1];
+            if (r.dstride == bytes && r.bytes == bytes * r.nf && d == r.dev + bytes * r.nf &&
+                h == r.host + bytes * r.nf) {   // both sides continue the run
+                r.nf++;
+                r.bytes += bytes;
+                return;
+            }
+        }
+        runs[n++] = Run{d, h, bytes, dstride, 1};
+    }
+    int run(cudaMemcpyKind kind, cudaStream_t st) {
+        for (int k = 0; k < n; ++k) {
+            const Run& r = runs[k];
+            if (kind == cudaMemcpyHostToDevice) QDFN_CUDA(cudaMemcpyAsync(r.dev, r.host, r.bytes, kind, st));
+            else QDFN_CUDA(cudaMemcpyAsync(r.host, r.dev, r.bytes, kind, st));
+        }
+        return QDFN_OK;
+    }
+};
+}  // namespace
+
 extern "C" int qdfn_set_state_all(qdfn_ctx* c, const double* V, const double* D, const double* theta,
                                   const double* friction, const double* accel, const double* sigma_old,
                                   const double* T, const double* dt, const int64_t* step, void* stream) {
@@ -1891,16 +1947,12 @@ extern "C" int qdfn_set_state_all(qdfn_ctx* c, const double* V, const double* D,
     if (c->running) return fail(QDFN_ERR_STATE, "a run is in flight (qdfn_sync or qdfn_get_state_all first)");
     cudaStream_t st = (cudaStream_t)stream;
     const size_t n = (size_t)c->R * c->N * 8, ns = (size_t)c->R * 8;
-    if (V) QDFN_CUDA(cudaMemcpyAsync(c->V, V, n, cudaMemcpyHostToDevice, st));
-    if (D) QDFN_CUDA(cudaMemcpyAsync(c->D, D, n, cudaMemcpyHostToDevice, st));
-    if (theta) QDFN_CUDA(cudaMemcpyAsync(c->theta, theta, n, cudaMemcpyHostToDevice, st));
-    if (friction) QDFN_CUDA(cudaMemcpyAsync(c->fric, friction, n, cudaMemcpyHostToDevice, st));
-    if (accel) QDFN_CUDA(cudaMemcpyAsync(c->accel, accel, n, cudaMemcpyHostToDevice, st));
-    if (sigma_old) QDFN_CUDA(cudaMemcpyAsync(c->sig_old, sigma_old, n, cudaMemcpyHostToDevice, st));
-    if (T) QDFN_CUDA(cudaMemcpyAsync(c->T, T, ns, cudaMemcpyHostToDevice, st));
-    if (dt) QDFN_CUDA(cudaMemcpyAsync(c->dt, dt, ns, cudaMemcpyHostToDevice, st));
-    if (step) QDFN_CUDA(cudaMemcpyAsync(c->step, step, ns, cudaMemcpyHostToDevice, st));
-    return QDFN_OK;
+    const size_t rn = (size_t)kernel_R(c->R) * c->N * 8, rs = (size_t)kernel_R(c->R) * 8;
+    CopyList cl;
+    cl.add(c->V, V, n, rn); cl.add(c->D, D, n, rn); cl.add(c->theta, theta, n, rn);
+    cl.add(c->fric, friction, n, rn); cl.add(c->accel, accel, n, rn); cl.add(c->sig_old, sigma_old, n, rn);
+    cl.add(c->T, T, ns, rs); cl.add(c->dt, dt, ns, rs); cl.add(c->step, step, ns, rs);
+    return cl.run(cudaMemcpyHostToDevice, st);
 }
 
 extern "C" int qdfn_get_state_all(qdfn_ctx* c, double* V, double* D, double* theta, double* friction,
@@ -1912,15 +1964,12 @@ extern "C" int qdfn_get_state_all(qdfn_ctx* c, double* V, double* D, double* the
     if (c->running && !completes) return fail(QDFN_ERR_STATE, "the run in flight is on another stream");
     if (completes && !wait) return fail(QDFN_ERR_INVALID, "reading the state of a run in flight needs wait=1");
     const size_t n = (size_t)c->R * c->N * 8, ns = (size_t)c->R * 8;
-    if (V) QDFN_CUDA(cudaMemcpyAsync(V, c->V, n, cudaMemcpyDeviceToHost, st));
-    if (D) QDFN_CUDA(cudaMemcpyAsync(D, c->D, n, cudaMemcpyDeviceToHost, st));
-    if (theta) QDFN_CUDA(cudaMemcpyAsync(theta, c->theta, n, cudaMemcpyDeviceToHost, st));
-    if (friction) QDFN_CUDA(cudaMemcpyAsync(friction, c->fric, n, cudaMemcpyDeviceToHost, st));
-    if (accel) QDFN_CUDA(cudaMemcpyAsync(accel, c->accel, n, cudaMemcpyDeviceToHost, st));
-    if (sigma_old) QDFN_CUDA(cudaMemcpyAsync(sigma_old, c->sig_old, n, cudaMemcpyDeviceToHost, st));
-    if (T) QDFN_CUDA(cudaMemcpyAsync(T, c->T, ns, cudaMemcpyDeviceToHost, st));
-    if (dt) QDFN_CUDA(cudaMemcpyAsync(dt, c->dt, ns, cudaMemcpyDeviceToHost, st));
-    if (step) QDFN_CUDA(cudaMemcpyAsync(step, c->step, ns, cudaMemcpyDeviceToHost, st));
+    const size_t rn = (size_t)kernel_R(c->R) * c->N * 8, rs = (size_t)kernel_R(c->R) * 8;
+    CopyList cl;
+    cl.add(c->V, V, n, rn); cl.add(c->D, D, n, rn); cl.add(c->theta, theta, n, rn);
+    cl.add(c->fric, friction, n, rn); cl.add(c->accel, accel, n, rn); cl.add(c->sig_old, sigma_old, n, rn);
+    cl.add(c->T, T, ns, rs); cl.add(c->dt, dt, ns, rs); cl.add(c->step, step, ns, rs);
+    if (int rc = cl.run(cudaMemcpyDeviceToHost, st)) return rc;
     if (completes) {   // the run's outcome travels with the state: one synchronisation
         if (!c->host_status) QDFN_CUDA(cudaHostAlloc(&c->host_status, (1 + kMaxInst) * sizeof(int), 0));
         QDFN_CUDA(cudaMemcpyAsync(c->host_status, c->gerr, sizeof(int), cudaMemcpyDeviceToHost, st));
