@@ -415,6 +415,43 @@ __device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
     return rb >= p.rb_small0 ? p.nchunk2 : p.nchunk;
 }
 
+// One matrix's half of sum_partials (side 0 shear, 1 normal), for a lane pair
+// that splits the two sums between its lanes; same order and arithmetic.
+template <bool kPairs>
+__device__ __forceinline__ double sum_partials_side(const SimParams& p, int r, int64_t i, int side) {
+    const int64_t cs = (int64_t)p.R * p.N;
+    const int64_t base = (int64_t)r * p.N + i;
+    const int nch = chunks_of_rb(p, i / p.ld);
+    const double* part = side == 0 ? p.part_s : p.part_n;
+    if constexpr (kPairs) {
+        const float2* ps = reinterpret_cast<const float2*>(part) + base;
+        float h = 0.f, l = 0.f;
+        int c = 0;
+        for (; c + 16 <= nch; c += 16) {
+            float2 t[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + (c + k) * cs);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) { two_sum_acc(h, l, t[k].x); l += t[k].y; }
+        }
+        for (; c < nch; ++c) { const float2 a = __ldcg(ps + c * cs); two_sum_acc(h, l, a.x); l += a.y; }
+        return (double)h + (double)l;
+    } else {
+        const double* ps = part + base;
+        double a = 0;
+        int c = 0;
+        for (; c + 16 <= nch; c += 16) {
+            double t[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + (c + k) * cs);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) a += t[k];
+        }
+        for (; c < nch; ++c) a += __ldcg(ps + c * cs);
+        return a;
+    }
+}
+
 template <bool kPairs>
 __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t i, double& ss,
                                              double& sn) {
@@ -868,7 +905,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 } else {
                     double ss, sn;
                     const uint64_t t_sp0 = globaltimer_ns();
-                    sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
+                    if (pair) {   // the even lane sums the shear partials, the odd lane the normal ones
+                        const unsigned pm = 3u << (threadIdx.x & 30);
+                        const double mine = sum_partials_side<sizeof(X) == 4>(p, r, i, (int)(threadIdx.x & 1));
+                        ss = __shfl_sync(pm, mine, (int)(threadIdx.x & 30));
+                        sn = __shfl_sync(pm, mine, (int)(threadIdx.x & 30) + 1);
+                    } else {
+                        sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
+                    }
                     t_sp = globaltimer_ns() - t_sp0;
                     if (writer) {
                         p.tld[q] = -ss;   // ELSM * (0 - DispOld)
