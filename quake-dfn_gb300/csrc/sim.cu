@@ -104,7 +104,8 @@ struct SimParams {
     double *V, *D, *theta, *fric, *accel, *sig_old;
     double *Vn, *Dn, *thn, *fn, *sn, *accel_n, *dtall, *tld, *knd;
     int *instab, *flag, *sw, *sw_n;
-    double *part_s, *part_n;         // [max(nchunk, nchunk2)][R][N]
+    double *part_s, *part_n;         // [2][max(nchunk, nchunk2)][R][N], by step parity
+    int64_t part_stride;             // elements of one of the two partial buffers
     // scalars [R]
     double *T, *dt;
     int64_t *step, *nrec;
@@ -114,8 +115,11 @@ struct SimParams {
     // barrier + reductions
     unsigned *bar_count, *bar_gen;
     double* red;                     // [2][nblocks][R][kRedSlots]
-    // per-step counters, [2] (and rb_done [2][rb_stride]) by step parity
+    // per-step counters, three sets used by steps s, s+1, s+2 (mod 3): [3], and
+    // rb_done / rb_solved [3][rb_stride]
     unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
+    unsigned long long* spec_ctr;    // tiles of the step streamed ahead during the step before
+    unsigned* rb_solved;             // dense: solved row chunks per row block
     unsigned* rb_done;               // dense: tile arrivals per row block (one per operator warp and tile)
     unsigned long long* solve_ctr;   // dense: row chunks handed to the solver warps
     int* gerr;
@@ -123,7 +127,8 @@ struct SimParams {
     unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
     int64_t n_rb;                    // dense: operator row blocks
     int hold_cap;                    // dense: row chunks a block may hold at once in the overlapped phase
-    unsigned long long* tmax;        // [2][4] per-step max over blocks of (operator end, solver end,
+    int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
+    unsigned long long* tmax;        // [3][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, chunk partial sums), ns
 };
 
@@ -310,6 +315,11 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 }
 // barrier of the operator role alone (named barrier 1, warps [0, kOpWarps))
 __device__ __forceinline__ void op_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kOpThreads) : "memory"); }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* ptr) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ptr) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* ptr) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
@@ -327,7 +337,7 @@ struct StageDesc {
     long long tile;   // operator tile, or -1: no tiles left (end marker)
     int q, nst;       // stage index within the tile, stages of the tile
     int seq;          // tile sequence number in this CTA (selects the x buffer)
-    int pad;
+    int next;         // 1: a tile of the next step (streamed ahead)
 };
 static_assert(6 * 8 + kStages * sizeof(StageDesc) <= kMbarBytes, "mbarriers + stage descriptors");
 
@@ -348,6 +358,7 @@ struct Pipe {
     uint32_t filled;
     long long ftile;         // tile being filled; -2 none yet, -1 no tiles left
     int fq, fnst, fseq;      // its next stage, its stage count, its sequence number
+    int fphase, fnext;       // 0 this step's tiles, 1 the next step's, 2 done; the tile's step
     uint32_t last_stage[2];  // last stage of the latest tile using each x buffer
 };
 constexpr uint32_t kNoStage = 0xffffffffu;
@@ -362,6 +373,8 @@ __device__ __forceinline__ void pipe_init(Pipe& pp, unsigned char* smem) {
     pp.ftile = -2;
     pp.fq = pp.fnst = 0;
     pp.fseq = -1;
+    pp.fphase = 0;
+    pp.fnext = 0;
     pp.last_stage[0] = pp.last_stage[1] = kNoStage;
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -418,9 +431,9 @@ __device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
 // One matrix's half of sum_partials (side 0 shear, 1 normal), for a lane pair
 // that splits the two sums between its lanes; same order and arithmetic.
 template <bool kPairs>
-__device__ __forceinline__ double sum_partials_side(const SimParams& p, int r, int64_t i, int side) {
+__device__ __forceinline__ double sum_partials_side(const SimParams& p, int r, int64_t i, int side, int ppar) {
     const int64_t cs = (int64_t)p.R * p.N;
-    const int64_t base = (int64_t)r * p.N + i;
+    const int64_t base = (int64_t)ppar * p.part_stride + (int64_t)r * p.N + i;
     const int nch = chunks_of_rb(p, i / p.ld);
     const double* part = side == 0 ? p.part_s : p.part_n;
     if constexpr (kPairs) {
@@ -453,10 +466,10 @@ __device__ __forceinline__ double sum_partials_side(const SimParams& p, int r, i
 }
 
 template <bool kPairs>
-__device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t i, double& ss,
-                                             double& sn) {
+__device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t i, double& ss, double& sn,
+                                             int ppar = 0) {
     const int64_t cs = (int64_t)p.R * p.N;
-    const int64_t base = (int64_t)r * p.N + i;
+    const int64_t base = (int64_t)ppar * p.part_stride + (int64_t)r * p.N + i;
     const int nch = chunks_of_rb(p, i / p.ld);
     if constexpr (kPairs) {
         const float2* ps = reinterpret_cast<const float2*>(p.part_s) + base;
@@ -517,14 +530,50 @@ __device__ __forceinline__ TileGeo tile_geo(const SimParams& p, int64_t nrb, int
     return g;
 }
 
-// Producer (thread 0): fill the next stage of the ring -- the next stage of the
-// tile being filled, the first stage of the next tile from the global counter
-// (with the tile's x chunk, from the instance-interleaved copy of D, in the
-// same transaction), or the end marker.  Returns false when a bounded wait
-// ran out.
+// What the producer and the operator warps need to know about a step.
+struct StepCtx {
+    int set, set_next;        // counter sets of this step and the next (mod 3)
+    int ppar;                 // partial buffer of this step; the next step's is ppar ^ 1
+    const void* xcur;         // x copy of D read by this step's tiles
+    const void* xnext;        // x copy the next step's tiles read (written by this step's solves)
+    long long spec_done;      // this step's tiles already streamed during the step before
+    int spec;                 // after this step's tiles, stream the next step's first column chunks
+};
+
+// Tiles of the next step streamed during a step's tail: column chunks
+// c < min(c_spec, nchunk) of the full-width row blocks, column-major
+// (u -> rb = u % nrb_reg, c = u / nrb_reg), so the x they need -- the slip of
+// the first patches, solved early in the step -- is ready first.
+__device__ __forceinline__ void spec_shape(const SimParams& p, int64_t nrb, int64_t* nrb_reg, int64_t* n_spec) {
+    *nrb_reg = min(p.rb_small0, nrb);
+    *n_spec = (int64_t)min(p.c_spec, p.nchunk) * *nrb_reg;
+}
+
+// Zero counter set s (tile and early-tile counters, solve chunk counter,
+// row-block completion and solved-chunk counts, diagnostics maxima).  Called by
+// every thread of one block, with no other block using the set.
+__device__ __forceinline__ void reset_counter_set(const SimParams& p, int s) {
+    if (threadIdx.x == 0) {
+        atomicExch(p.tile_ctr + s, 0ull);
+        atomicExch(p.spec_ctr + s, 0ull);
+        atomicExch(p.solve_ctr + s, 0ull);
+    }
+    unsigned* a = p.rb_done + (int64_t)s * p.rb_stride;
+    unsigned* b = p.rb_solved + (int64_t)s * p.rb_stride;
+    for (int64_t k = threadIdx.x; k < p.n_rb; k += blockDim.x) { a[k] = 0u; b[k] = 0u; }
+    if (threadIdx.x < 4) p.tmax[s * 4 + threadIdx.x] = 0ull;
+}
+
+// Producer (one lane): fill the next stage of the ring -- the next stage of the
+// tile being filled, else the first stage of the next tile: this step's tiles
+// from the global counter (skipping those streamed during the step before),
+// then, when the step streams ahead, the next step's first column chunks once
+// the slip they read is solved, then the end marker.  A tile's first stage
+// also carries its x chunk, from the instance-interleaved copy of D.  Returns
+// false when a bounded wait ran out.
 template <class M, int R>
 __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, typename M::X* xs, int64_t nrb,
-                              int64_t ntiles, uint64_t pol, int cpar, const typename M::X* xdc) {
+                                              int64_t ntiles, uint64_t pol, const StepCtx& sc) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int EB = kGranule / VEC;   // bytes per stored entry
@@ -535,13 +584,42 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     if (n >= (uint32_t)kStages && !mbar_wait(pp.empty + slot, ((n - kStages) / kStages) & 1u, kWaitLimitNs))
         return false;
     if (pp.ftile == -2 || (pp.ftile >= 0 && pp.fq >= pp.fnst)) {
-        const long long t = (long long)atomicAdd(p.tile_ctr + cpar, 1ull);
-        if (t >= ntiles) {
-            pp.ftile = -1;
-        } else {
+        int64_t nrb_reg, n_spec;
+        spec_shape(p, nrb, &nrb_reg, &n_spec);
+        const int64_t cs = min(p.c_spec, p.nchunk);
+        pp.ftile = -1;
+        while (pp.fphase < 2) {
+            if (pp.fphase == 0) {            // this step
+                const long long t = (long long)atomicAdd(p.tile_ctr + sc.set, 1ull);
+                if (t >= ntiles) { pp.fphase = (sc.spec && n_spec > 0) ? 1 : 2; continue; }
+                const TileGeo g = tile_geo(p, nrb, t);
+                if (g.rb < nrb_reg && g.c < cs && (int64_t)g.c * nrb_reg + g.rb < sc.spec_done) continue;
+                pp.ftile = t;
+                pp.fnext = 0;
+                break;
+            }
+            // the next step (fphase 1)
+            const long long u = (long long)atomicAdd(p.spec_ctr + sc.set_next, 1ull);
+            if (u >= n_spec) { pp.fphase = 2; continue; }
+            const int64_t rb = u % nrb_reg, c = u / nrb_reg;
+            const long long t = rb * p.nchunk + c;
+            // its x chunk: the slip of patches [j0, j0 + L), solved in this step
+            const TileGeo g = tile_geo(p, nrb, t);
+            const unsigned need = (unsigned)(R * (rows_per_blk / 16));   // solve chunks per row block
+            const uint64_t t0 = globaltimer_ns();
+            for (int64_t b = g.j0 / rows_per_blk; b <= (int64_t)(g.j0 + g.L - 1) / rows_per_blk; ++b)
+                while (ld_acquire_u32(p.rb_solved + sc.set * p.rb_stride + b) < need) {
+                    if (globaltimer_ns() - t0 > kWaitLimitNs || *(volatile int*)p.gerr != 0) return false;
+                    __nanosleep(200);
+                }
+            fence_proxy_async_global();
             pp.ftile = t;
+            pp.fnext = 1;
+            break;
+        }
+        if (pp.ftile >= 0) {
             pp.fq = 0;
-            pp.fnst = tile_geo(p, nrb, t).nst;
+            pp.fnst = tile_geo(p, nrb, pp.ftile).nst;
             pp.fseq++;
         }
     }
@@ -568,6 +646,7 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     d->q = q;
     d->nst = g.nst;
     d->seq = pp.fseq;
+    d->next = pp.fnext;
     const int nc = (int)min((int64_t)kColsPerStage, g.L - (int64_t)q * kColsPerStage);
     const uint32_t bytes = (uint32_t)nc * kSegBytes;
     // x: the tile's columns rounded up to 4 (the copy is padded past N)
@@ -581,36 +660,39 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     bulk_g2s(st, reinterpret_cast<const unsigned char*>(p.E) + off, bytes, m, pol);
     bulk_g2s(st + (size_t)kColsPerStage * kSegBytes, reinterpret_cast<const unsigned char*>(p.Kn) + off, bytes, m,
              pol);
-    if (q == 0)
-        bulk_g2s(xs + (size_t)xb * p.xbuf, xdc + (int64_t)g.j0 * R, xbytes, m, pol);
+    if (q == 0) {
+        const X* xsrc = reinterpret_cast<const X*>(pp.fnext ? sc.xnext : sc.xcur);
+        bulk_g2s(xs + (size_t)xb * p.xbuf, xsrc + (int64_t)g.j0 * R, xbytes, m, pol);
+    }
     if (q == g.nst - 1) pp.last_stage[xb] = n;
     pp.fq = q + 1;
     pp.filled = n + 1;
     return true;
 }
 
-// Producer role (one lane of warp kProducerWarp): walk this step's tiles and
-// keep the ring full -- every fill waits only for the release of the slot's
+// Producer role (one lane of warp kProducerWarp): walk this step's tiles (and
+// the next step's first column chunks when the step streams ahead) and keep
+// the ring full -- every fill waits only for the release of the slot's
 // previous stage by the operator warps -- until the end marker is issued.  On
 // a failed wait it drains the copies it issued (bounded) and returns false.
 template <class M, int R>
-__device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs, int cpar,
-                              const typename M::X* xdc) {
+__device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs, const StepCtx& sc) {
     constexpr int64_t rows_per_blk = (int64_t)kOpThreads * M::VEC;
     const int64_t nrb = (p.N + rows_per_blk - 1) / rows_per_blk;
     const int64_t ntiles = min(p.rb_small0, nrb) * p.nchunk + (nrb - min(p.rb_small0, nrb)) * p.nchunk2;
     const uint64_t pol = l2_evict_first_policy();
     fence_proxy_async_global();
     pp.ftile = -2;
-    while (pp.ftile != -1) {
-        if (!produce_stage<M, R>(p, pp, xs, nrb, ntiles, pol, cpar, xdc)) {
+    pp.fphase = 0;
+    do {
+        if (!produce_stage<M, R>(p, pp, xs, nrb, ntiles, pol, sc)) {
             atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
             const uint32_t from = pp.filled > (uint32_t)kStages ? pp.filled - kStages : 0u;
             for (uint32_t k = from; k < pp.filled; ++k)
                 mbar_wait(pp.full + (k % kStages), (k / kStages) & 1u, kWaitLimitNs);
             return false;
         }
-    }
+    } while (pp.ftile != -1);
     return true;
 }
 
@@ -620,7 +702,7 @@ __device__ bool produce_tiles(const SimParams& p, Pipe& pp, typename M::X* xs, i
 // writes its partials, and each warp then counts itself into the row block's
 // completion counter (kOpWarps arrivals per tile).
 template <class M, int R>
-__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, int cpar) {
+__device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, const StepCtx& sc) {
     using X = typename M::X;
     constexpr int VEC = M::VEC;
     constexpr int64_t rows_per_blk = (int64_t)kOpThreads * VEC;
@@ -699,7 +781,9 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, in
                     for (int v = 0; v < VEC; ++v) {
                         const int64_t i = i0 + v;
                         if (i < N) {
-                            const int64_t o = ((int64_t)g.c * R + r) * N + i;
+                            // the tile's step selects the partial buffer
+                            const int64_t o = (int64_t)(sc.ppar ^ d.next) * p.part_stride +
+                                              ((int64_t)g.c * R + r) * N + i;
                             if constexpr (sizeof(X) == 8) {
                                 p.part_s[o] = fs[r][v];
                                 p.part_n[o] = fn[r][v];
@@ -712,7 +796,8 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, in
             }
             __threadfence();
             __syncwarp();
-            if ((threadIdx.x & 31) == 0) atomicAdd(p.rb_done + cpar * p.rb_stride + g.rb, 1u);
+            if ((threadIdx.x & 31) == 0)
+                atomicAdd(p.rb_done + (d.next ? sc.set_next : sc.set) * p.rb_stride + g.rb, 1u);
         }
     }
     if (!ok) {   // the producer drains the copies it issued
@@ -848,11 +933,11 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 s[4] = v[r][0]; s[5] = v[r][1]; s[6] = v[r][2]; s[7] = v[r][3];
                 s[8] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
             }
-            if (blockIdx.x == 0) { atomicExch(p.tile_ctr, 0ull); atomicExch(p.solve_ctr, 0ull); }
+            if (blockIdx.x == 0 && HM) atomicExch(p.tile_ctr, 0ull);
         }
-        if (!HM && blockIdx.x == 0) {   // step 0's counter set
-            for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) p.rb_done[k] = 0u;
-            if (threadIdx.x < 4) p.tmax[threadIdx.x] = 0ull;
+        if (!HM && blockIdx.x == 0) {   // the counter sets of steps 0 and 1
+            reset_counter_set(p, 0);
+            reset_counter_set(p, 1);
             __threadfence();
         }
         if (!grid_barrier(p, deadline)) return;
@@ -880,11 +965,18 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (stop) break;
         }
         const int par = s_par;             // which buffer holds the current state
-        const int cpar = (int)(it & 1);    // which counter set this step uses
+        const int cpar = (int)(it % 3);    // which counter set this step uses (the next step: +1 mod 3)
+        const int cnext = (int)((it + 1) % 3);
         if (threadIdx.x < R) s_done[threadIdx.x] = 0;
         red_init();
         __syncthreads();
         const X* xdc = reinterpret_cast<const X*>(p.xd) + (size_t)par * p.xd_stride;
+        // FP32/BF16: after its own tiles a step streams the next step's first
+        // column chunks (not on the last step of a launch, whose next step
+        // belongs to another launch)
+        StepCtx sc{cpar, cnext, (int)(it & 1), xdc,
+                   reinterpret_cast<const X*>(p.xd) + (size_t)(par ^ 1) * p.xd_stride, 0,
+                   (!HM && sizeof(X) == 4 && p.c_spec > 0 && it + 1 < nsteps) ? 1 : 0};
         // one (instance r, patch i) item of a solve pass; pass 0 of a step also
         // forms the row's operator products.  pair: the item runs on a lane
         // pair (lanes 2k, 2k+1, both called with it); the even lane writes the
@@ -907,11 +999,11 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     const uint64_t t_sp0 = globaltimer_ns();
                     if (pair) {   // the even lane sums the shear partials, the odd lane the normal ones
                         const unsigned pm = 3u << (threadIdx.x & 30);
-                        const double mine = sum_partials_side<sizeof(X) == 4>(p, r, i, (int)(threadIdx.x & 1));
+                        const double mine = sum_partials_side<sizeof(X) == 4>(p, r, i, (int)(threadIdx.x & 1), sc.ppar);
                         ss = __shfl_sync(pm, mine, (int)(threadIdx.x & 30));
                         sn = __shfl_sync(pm, mine, (int)(threadIdx.x & 30) + 1);
                     } else {
-                        sum_partials<sizeof(X) == 4>(p, r, i, ss, sn);
+                        sum_partials<sizeof(X) == 4>(p, r, i, ss, sn, sc.ppar);
                     }
                     t_sp = globaltimer_ns() - t_sp0;
                     if (writer) {
@@ -1009,9 +1101,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
             if ((threadIdx.x >> 5) < kOpWarps) {
-                if (!dense_matvec<M, R>(p, pipe, xs, cpar)) s_op_fail = 1;
+                if (!dense_matvec<M, R>(p, pipe, xs, sc)) s_op_fail = 1;
             } else if (threadIdx.x == kProducerWarp * 32) {
-                if (!produce_tiles<M, R>(p, pipe, xs, cpar, xdc)) s_op_fail = 1;
+                if (!produce_tiles<M, R>(p, pipe, xs, sc)) s_op_fail = 1;
             }
             if (threadIdx.x == 0) s_tm[6] += globaltimer_ns() - t_f0;
             __syncthreads();
@@ -1034,7 +1126,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
             bool solve = true;
             if (warp < kOpWarps) {
-                if (!dense_matvec<M, R>(p, pipe, xs, cpar)) { s_fused_fail = 1; solve = false; }
+                if (!dense_matvec<M, R>(p, pipe, xs, sc)) { s_fused_fail = 1; solve = false; }
                 if (threadIdx.x == 0) {
                     const uint64_t d = globaltimer_ns() - t_f0;
                     s_tm[6] += d;
@@ -1042,7 +1134,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 }
             } else if (warp == kProducerWarp) {   // lane 0 fills the ring, then the warp solves
                 int pok = 1;
-                if (lane == 0) pok = produce_tiles<M, R>(p, pipe, xs, cpar, xdc) ? 1 : 0;
+                if (lane == 0) {
+                    // this step's tiles already streamed during the step before
+                    int64_t nrb_reg, n_spec;
+                    spec_shape(p, p.n_rb, &nrb_reg, &n_spec);
+                    sc.spec_done = (long long)min((int64_t)ld_acquire_u64(p.spec_ctr + cpar), n_spec);
+                    pok = produce_tiles<M, R>(p, pipe, xs, sc) ? 1 : 0;
+                }
                 pok = __shfl_sync(0xffffffffu, pok, 0);
                 if (!pok) { s_fused_fail = 1; solve = false; }
             }
@@ -1110,6 +1208,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     __syncwarp();
                     if (lane == 0) {
                         atomicSub(&s_held, 1);
+                        __threadfence();   // the chunk's x copy of D is written (and proxy-fenced)
+                        atomicAdd(p.rb_solved + cpar * p.rb_stride + rb, 1u);
                         atomicMax(p.tmax + cpar * 4 + 2, (unsigned long long)(globaltimer_ns() - t_ready));
                         atomicMax(p.tmax + cpar * 4 + 3, (unsigned long long)t_sp);
                     }
@@ -1145,13 +1245,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     solve_item(q, r, q - (int64_t)r * N, first != 0, false);
                 }
             }
-            if (first && !HM && blockIdx.x == 0) {
-                // reset the other counter set for the next step: its last use was
-                // the previous step, which every block has left
-                if (threadIdx.x == 0) { atomicExch(p.tile_ctr + (cpar ^ 1), 0ull); atomicExch(p.solve_ctr + (cpar ^ 1), 0ull); }
-                unsigned* rbn = p.rb_done + (cpar ^ 1) * p.rb_stride;
-                for (int64_t k = threadIdx.x; k < p.n_rb; k += kSimThreads) rbn[k] = 0u;
-                if (threadIdx.x < 4) p.tmax[(cpar ^ 1) * 4 + threadIdx.x] = 0ull;
+            if (!HM && blockIdx.x == 0 && (first || s_iter == 1)) {
+                // pass 0: reset the counter set of the step after next (its last
+                // use was the previous step, which every block has left; the
+                // next step's early tiles will use it during the next step).
+                // First retry pass: this step's slip changes, so the next step's
+                // early tiles are discarded -- their counters start again
+                reset_counter_set(p, first ? (int)((it + 2) % 3) : cnext);
                 __threadfence();
             }
             __syncthreads();
@@ -1316,8 +1416,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_apply(SimParams p) {
     pipe_init(pipe, smem_raw);
     X* xs = reinterpret_cast<X*>(smem_raw + kPipeBytes + kMbarBytes);
     const int warp = threadIdx.x >> 5;
-    if (warp < kOpWarps) dense_matvec<M, R>(p, pipe, xs, 0);          // the operator role
-    else if (threadIdx.x == kProducerWarp * 32) produce_tiles<M, R>(p, pipe, xs, 0, reinterpret_cast<const X*>(p.xd));
+    const StepCtx sc{0, 1, 0, p.xd, p.xd, 0, 0};
+    if (warp < kOpWarps) dense_matvec<M, R>(p, pipe, xs, sc);          // the operator role
+    else if (threadIdx.x == kProducerWarp * 32) produce_tiles<M, R>(p, pipe, xs, sc);
 }
 
 template <class X, int R>
@@ -1428,7 +1529,10 @@ struct qdfn_ctx {
     unsigned long long* prof;
     unsigned long long* tile_ctr;
     unsigned long long* solve_ctr;
+    unsigned long long* spec_ctr;
     unsigned* rb_done;
+    unsigned* rb_solved;
+    int64_t part_stride = 0;
     unsigned long long* tmax;
     void* E = nullptr;
     void* Kn = nullptr;
@@ -1440,6 +1544,7 @@ struct qdfn_ctx {
     int64_t xbuf = 0;                // elements per shared-memory x buffer
     int64_t xd_stride = 0, rb_stride = 0;
     int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
+    int c_spec = 8;                  // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS)
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1498,7 +1603,8 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.Vn = c->Vn; p.Dn = c->Dn; p.thn = c->thn; p.fn = c->fn; p.sn = c->sn; p.dtall = c->dtall;
     p.tld = c->tld; p.knd = c->knd; p.instab = c->instab; p.flag = c->flag; p.sw = c->sw;
     p.sw_n = c->sw_n; p.accel_n = c->accel_n;
-    p.part_s = c->part_s; p.part_n = c->part_n;
+    p.part_s = c->part_s; p.part_n = c->part_n; p.part_stride = c->part_stride;
+    p.spec_ctr = c->spec_ctr; p.rb_solved = c->rb_solved; p.c_spec = c->c_spec;
     p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
@@ -1575,9 +1681,10 @@ int configure_launch(qdfn_ctx* c) {
         const int64_t rows_per_blk = (int64_t)kOpThreads * vec;
         const int64_t nrb = (c->N + rows_per_blk - 1) / rows_per_blk;
         // tiles per SM and step before the guided tail (tuning knob QDFN_TILES_PER_SM)
-        int64_t tiles_per_sm = 3;
+        int64_t tiles_per_sm = 4;
         if (const char* e = std::getenv("QDFN_TILES_PER_SM")) tiles_per_sm = std::max(1, std::min(64, std::atoi(e)));
         if (const char* e = std::getenv("QDFN_SOLVE_HOLD")) c->hold_cap = std::max(1, std::min(64, std::atoi(e)));
+        if (const char* e = std::getenv("QDFN_SPEC_COLS")) c->c_spec = std::max(0, std::min(64, std::atoi(e)));
         int64_t want_chunks = std::max<int64_t>(1, (tiles_per_sm * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
         // two x buffers (R x chunk x elem each) share the 227 KB with the 192 KB stage ring
@@ -1635,8 +1742,9 @@ int configure_launch(qdfn_ctx* c) {
         if ((reinterpret_cast<uintptr_t>(c->xd) | (uintptr_t)(c->xd_stride * xsz)) % 16 != 0)
             return fail(QDFN_ERR_INVALID, "x copy of D not 16-byte aligned");
         const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
-        if ((rc = c->dalloc(&c->part_s, slots * Rk * c->N))) return rc;
-        if ((rc = c->dalloc(&c->part_n, slots * Rk * c->N))) return rc;
+        c->part_stride = (int64_t)slots * Rk * c->N;   // two buffers: this step's and the next's
+        if ((rc = c->dalloc(&c->part_s, 2 * (size_t)c->part_stride))) return rc;
+        if ((rc = c->dalloc(&c->part_n, 2 * (size_t)c->part_stride))) return rc;
     }
     if ((rc = c->dalloc(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots))) return rc;
     return QDFN_OK;
@@ -1690,10 +1798,10 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
         c->bar_count = reinterpret_cast<unsigned*>(ctrl + 1);
         c->bar_gen = reinterpret_cast<unsigned*>(ctrl + 2);
     }
-    A(prof, kCounters); A(tile_ctr, 2);
+    A(prof, kCounters); A(tile_ctr, 3); A(spec_ctr, 3);
     // per-step counters, two sets used by alternate steps (one is reset while the other runs)
     c->rb_stride = (N + kOpThreads - 1) / kOpThreads;   // row blocks have >= kOpThreads rows
-    A(solve_ctr, 2); A(tmax, 8); A(rb_done, 2 * (size_t)c->rb_stride);
+    A(solve_ctr, 3); A(tmax, 12); A(rb_done, 3 * (size_t)c->rb_stride); A(rb_solved, 3 * (size_t)c->rb_stride);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
