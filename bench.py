@@ -382,7 +382,7 @@ def run_ours(args):
                                        phases["ns_operator_warps_slowest"] / 1e6 / args.steps,
                                    "slowest_block_solver_warps": phases["ns_solver_warps_slowest"] / 1e6 / args.steps,
                                    "longest_chunk_solve": phases["ns_chunk_solve_longest"] / 1e6 / args.steps,
-                                   "longest_chunk_partial_sums": phases["ns_chunk_partials_longest"] / 1e6 / args.steps,
+                                   "last_row_block_complete": phases["ns_last_row_block"] / 1e6 / args.steps,
                                    "solve_reduce_and_retries": phases["ns_solve"] / 1e6 / args.steps,
                                    "block0_retry_solves": phases["ns_solve_own"] / 1e6 / args.steps,
                                    "block0_barrier_wait": phases["ns_solve_wait"] / 1e6 / args.steps,

@@ -198,8 +198,9 @@ int qdfn_get_blocks(const qdfn_ctx* ctx);
  * operator warps / solver warps spent in the overlapped operator-and-solve
  * phase (FP32/BF16 dense operator), [14]/[15] the same for the slowest block of
  * each step, [16] the longest time from a row block being complete to one of
- * its row chunks being solved, [17] the longest partial-sum time of a row
- * (per-step maxima, summed over steps). */
+ * its row chunks being solved, [17] the time from a block's start of the
+ * overlapped phase to the step's last row block being complete (per-step
+ * maxima, summed over steps). */
 int qdfn_get_counters(const qdfn_ctx* ctx, int64_t* out, int n);
 
 /* State of one instance (host copies).  Any pointer may be NULL. */

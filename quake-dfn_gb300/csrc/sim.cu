@@ -120,6 +120,7 @@ struct SimParams {
     unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
     unsigned long long* spec_ctr;    // tiles of the step streamed ahead during the step before
     unsigned* rb_solved;             // dense: solved row chunks per row block
+    unsigned* rb_hot;                // dense: row block holds a patch on the high-velocity solver next step
     unsigned* rb_done;               // dense: tile arrivals per row block (one per operator warp and tile)
     unsigned long long* solve_ctr;   // dense: row chunks handed to the solver warps
     int* gerr;
@@ -127,6 +128,8 @@ struct SimParams {
     unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
     int64_t n_rb;                    // dense: operator row blocks
     int hold_cap;                    // dense: row chunks a block may hold at once in the overlapped phase
+    int pair_solve;                  // overlapped phase: one lane pair per patch (else the even lanes alone)
+    int rb_ordered;                  // FP32/BF16 dense: row blocks with high-velocity patches first
     int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
     unsigned long long* tmax;        // [3][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, chunk partial sums), ns
@@ -538,7 +541,41 @@ struct StepCtx {
     const void* xnext;        // x copy the next step's tiles read (written by this step's solves)
     long long spec_done;      // this step's tiles already streamed during the step before
     int spec;                 // after this step's tiles, stream the next step's first column chunks
+    uint64_t t0;              // %globaltimer at the block's start of the phase (diagnostics)
+    const unsigned short* order;   // row-block order of the step's tiles (null: index order)
 };
+
+// Tile index of column chunk c of row block rb (the inverse of tile_geo).
+__device__ __forceinline__ long long tile_index(const SimParams& p, int64_t nrb, int64_t rb, int64_t c) {
+    const int64_t nrb_big = min(p.rb_small0, nrb);
+    return rb < nrb_big ? rb * p.nchunk + c : nrb_big * p.nchunk + (rb - nrb_big) * p.nchunk2 + c;
+}
+
+// Row-block order of a step (warp 0 of each block, the same in every block):
+// among the full-width row blocks, and among the narrow-tile ones after them,
+// the blocks holding a patch that starts the step on the high-velocity solver
+// come first, each group in index order.  Their solves take several times
+// longer than the others (tens of secant iterations), so they should start
+// early in the stream rather than finish after it.  The order only decides
+// when tiles and row chunks are taken, not what they compute.
+constexpr int kMaxOrder = 256;
+__device__ void rb_order(const SimParams& p, int set, unsigned short* order) {
+    const int lane = threadIdx.x & 31;
+    const int nrb = (int)p.n_rb, s0 = (int)min(p.rb_small0, (int64_t)nrb);
+    const unsigned* hot = p.rb_hot + (int64_t)set * p.rb_stride;
+    int pos = 0;
+    for (int grp = 0; grp < 2; ++grp) {
+        const int lo = grp ? s0 : 0, hi = grp ? nrb : s0;
+        for (int want = 1; want >= 0; --want)
+            for (int b0 = lo; b0 < hi; b0 += 32) {
+                const int b = b0 + lane;
+                const bool take = b < hi && ((__ldcg(hot + b) != 0u) == (want == 1));
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                if (take) order[pos + __popc(m & ((1u << lane) - 1u))] = (unsigned short)b;
+                pos += __popc(m);
+            }
+    }
+}
 
 // Tiles of the next step streamed during a step's tail: column chunks
 // c < min(c_spec, nchunk) of the full-width row blocks, column-major
@@ -550,9 +587,10 @@ __device__ __forceinline__ void spec_shape(const SimParams& p, int64_t nrb, int6
 }
 
 // Zero counter set s (tile and early-tile counters, solve chunk counter,
-// row-block completion and solved-chunk counts, diagnostics maxima).  Called by
-// every thread of one block, with no other block using the set.
-__device__ __forceinline__ void reset_counter_set(const SimParams& p, int s) {
+// row-block completion and solved-chunk counts, diagnostics maxima and, with
+// `hot`, the row-block order flags).  Called by every thread of one block, with
+// no other block using the set.
+__device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, bool hot) {
     if (threadIdx.x == 0) {
         atomicExch(p.tile_ctr + s, 0ull);
         atomicExch(p.spec_ctr + s, 0ull);
@@ -560,7 +598,12 @@ __device__ __forceinline__ void reset_counter_set(const SimParams& p, int s) {
     }
     unsigned* a = p.rb_done + (int64_t)s * p.rb_stride;
     unsigned* b = p.rb_solved + (int64_t)s * p.rb_stride;
-    for (int64_t k = threadIdx.x; k < p.n_rb; k += blockDim.x) { a[k] = 0u; b[k] = 0u; }
+    unsigned* h = p.rb_hot + (int64_t)s * p.rb_stride;
+    for (int64_t k = threadIdx.x; k < p.n_rb; k += blockDim.x) {
+        a[k] = 0u;
+        b[k] = 0u;
+        if (hot) h[k] = 0u;
+    }
     if (threadIdx.x < 4) p.tmax[s * 4 + threadIdx.x] = 0ull;
 }
 
@@ -590,9 +633,13 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
         pp.ftile = -1;
         while (pp.fphase < 2) {
             if (pp.fphase == 0) {            // this step
-                const long long t = (long long)atomicAdd(p.tile_ctr + sc.set, 1ull);
+                long long t = (long long)atomicAdd(p.tile_ctr + sc.set, 1ull);
                 if (t >= ntiles) { pp.fphase = (sc.spec && n_spec > 0) ? 1 : 2; continue; }
-                const TileGeo g = tile_geo(p, nrb, t);
+                TileGeo g = tile_geo(p, nrb, t);
+                if (sc.order) {   // the g.rb-th row block of the step's order (same tile shape)
+                    t = tile_index(p, nrb, sc.order[g.rb], g.c);
+                    g = tile_geo(p, nrb, t);
+                }
                 if (g.rb < nrb_reg && g.c < cs && (int64_t)g.c * nrb_reg + g.rb < sc.spec_done) continue;
                 pp.ftile = t;
                 pp.fnext = 0;
@@ -796,8 +843,12 @@ __device__ bool dense_matvec(const SimParams& p, Pipe& pp, typename M::X* xs, co
             }
             __threadfence();
             __syncwarp();
-            if ((threadIdx.x & 31) == 0)
-                atomicAdd(p.rb_done + (d.next ? sc.set_next : sc.set) * p.rb_stride + g.rb, 1u);
+            if ((threadIdx.x & 31) == 0) {
+                const unsigned old = atomicAdd(p.rb_done + (d.next ? sc.set_next : sc.set) * p.rb_stride + g.rb, 1u);
+                // diagnostics: when the step's last row block became complete
+                if (!d.next && sc.t0 != 0 && old + 1 == (unsigned)chunks_of_rb(p, g.rb) * kOpWarps)
+                    atomicMax(p.tmax + sc.set * 4 + 3, (unsigned long long)(globaltimer_ns() - sc.t0));
+            }
         }
     }
     if (!ok) {   // the producer drains the copies it issued
@@ -936,8 +987,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (blockIdx.x == 0 && HM) atomicExch(p.tile_ctr, 0ull);
         }
         if (!HM && blockIdx.x == 0) {   // the counter sets of steps 0 and 1
-            reset_counter_set(p, 0);
-            reset_counter_set(p, 1);
+            reset_counter_set(p, 0, true);
+            reset_counter_set(p, 1, true);
             __threadfence();
         }
         if (!grid_barrier(p, deadline)) return;
@@ -968,6 +1019,11 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         const int cpar = (int)(it % 3);    // which counter set this step uses (the next step: +1 mod 3)
         const int cnext = (int)((it + 1) % 3);
         if (threadIdx.x < R) s_done[threadIdx.x] = 0;
+        // FP32/BF16 dense: the step's row-block order (rows that start on the
+        // high-velocity solver first), from flags the previous step's solves set
+        __shared__ unsigned short s_order[kMaxOrder];
+        const bool use_order = !HM && sizeof(X) == 4 && p.rb_ordered && p.n_rb <= kMaxOrder;
+        if (use_order && threadIdx.x < 32) rb_order(p, cpar, s_order);
         red_init();
         __syncthreads();
         const X* xdc = reinterpret_cast<const X*>(p.xd) + (size_t)par * p.xd_stride;
@@ -977,12 +1033,12 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         StepCtx sc{cpar, cnext, (int)(it & 1), xdc,
                    reinterpret_cast<const X*>(p.xd) + (size_t)(par ^ 1) * p.xd_stride, 0,
                    (!HM && sizeof(X) == 4 && p.c_spec > 0 && it + 1 < nsteps) ? 1 : 0};
+        sc.order = use_order ? s_order : nullptr;
         // one (instance r, patch i) item of a solve pass; pass 0 of a step also
         // forms the row's operator products.  pair: the item runs on a lane
         // pair (lanes 2k, 2k+1, both called with it); the even lane writes the
         // results, the next step's solver switch and Accel, and this item's
         // share of the step reductions.
-        uint64_t t_sp = 0;   // duration of the last item's partial sums (diagnostics)
         // buffer pointers are selected where used, so none is held across the solve
 #define QDFN_CUR(a, b) (par ? p.b : p.a)
 #define QDFN_NXT(a, b) (par ? p.a : p.b)
@@ -996,7 +1052,6 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
                 } else {
                     double ss, sn;
-                    const uint64_t t_sp0 = globaltimer_ns();
                     if (pair) {   // the even lane sums the shear partials, the odd lane the normal ones
                         const unsigned pm = 3u << (threadIdx.x & 30);
                         const double mine = sum_partials_side<sizeof(X) == 4>(p, r, i, (int)(threadIdx.x & 1), sc.ppar);
@@ -1005,7 +1060,6 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     } else {
                         sum_partials<sizeof(X) == 4>(p, r, i, ss, sn, sc.ppar);
                     }
-                    t_sp = globaltimer_ns() - t_sp0;
                     if (writer) {
                         p.tld[q] = -ss;   // ELSM * (0 - DispOld)
                         p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
@@ -1035,10 +1089,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 sim::PatchOut o;
                 const int swq = QDFN_CUR(sw, sw_n)[q];
                 if (swq == 1) {
-                    if (!writer) return;   // the high-velocity solver runs on one lane
-                    o = sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err);
+                    o = pair ? sim::solve_highv_pair(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err)
+                             : sim::solve_highv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, err);
                 } else if (pair) {
-                    o = sim::solve_lowv_t<true>(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
+                    o = sim::solve_lowv_pair(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
                 } else {
                     o = sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
                 }
@@ -1077,6 +1131,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             const double A = (Vnew - VOld) / Dt;
             QDFN_NXT(accel, accel_n)[q] = A;
             QDFN_NXT(sw, sw_n)[q] = Vnew > p.switch_v ? 1 : 0;
+            if constexpr (!HM) {   // the next step streams and solves this row block early
+                if (Vnew > p.switch_v) atomicOr(p.rb_hot + cnext * p.rb_stride + i / p.ld, 1u);
+            }
             if (p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns)) {
                 if (isnan(Vnew)) red_max(r, 5, 1.0);
                 else red_max(r, 4, Vnew);
@@ -1100,6 +1157,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (threadIdx.x == 0) s_op_fail = 0;
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
+            sc.t0 = t_f0;
             if ((threadIdx.x >> 5) < kOpWarps) {
                 if (!dense_matvec<M, R>(p, pipe, xs, sc)) s_op_fail = 1;
             } else if (threadIdx.x == kProducerWarp * 32) {
@@ -1123,6 +1181,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; s_held = 0; }
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
+            sc.t0 = t_f0;
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
             bool solve = true;
             if (warp < kOpWarps) {
@@ -1180,7 +1239,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         if (lane == 0) atomicSub(&s_held, 1);
                         break;
                     }
-                    const int64_t rb = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
+                    const int64_t rbp = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
+                    const int64_t rb = sc.order ? (int64_t)sc.order[rbp] : rbp;   // in the step's order
                     const int r = (int)(rem / cpr);
                     const int64_t i = rb * rpb + (rem % cpr) * 16 + (lane >> 1);
                     int ok = 1;
@@ -1204,14 +1264,16 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         break;
                     }
                     const uint64_t t_ready = globaltimer_ns();
-                    if (i < N) solve_item((int64_t)r * N + i, r, i, true, true);
+                    // QDFN_PAIR_SOLVE=0: the even lane alone solves the patch with the
+                    // one-lane solver (same results; the lane-pair check uses it)
+                    if (i < N && (p.pair_solve || (lane & 1) == 0))
+                        solve_item((int64_t)r * N + i, r, i, true, p.pair_solve != 0);
                     __syncwarp();
                     if (lane == 0) {
                         atomicSub(&s_held, 1);
                         __threadfence();   // the chunk's x copy of D is written (and proxy-fenced)
                         atomicAdd(p.rb_solved + cpar * p.rb_stride + rb, 1u);
                         atomicMax(p.tmax + cpar * 4 + 2, (unsigned long long)(globaltimer_ns() - t_ready));
-                        atomicMax(p.tmax + cpar * 4 + 3, (unsigned long long)t_sp);
                     }
                 }
                 if (lane == 0) atomicMax(&s_t_solve, (unsigned long long)(globaltimer_ns() - t_f0));
@@ -1250,8 +1312,10 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 // use was the previous step, which every block has left; the
                 // next step's early tiles will use it during the next step).
                 // First retry pass: this step's slip changes, so the next step's
-                // early tiles are discarded -- their counters start again
-                reset_counter_set(p, first ? (int)((it + 2) % 3) : cnext);
+                // early tiles are discarded -- their counters start again (the
+                // order flags stay: the retry's solves add to them, and the
+                // order only decides when work is taken, not its result)
+                reset_counter_set(p, first ? (int)((it + 2) % 3) : cnext, first);
                 __threadfence();
             }
             __syncthreads();
@@ -1532,6 +1596,7 @@ struct qdfn_ctx {
     unsigned long long* spec_ctr;
     unsigned* rb_done;
     unsigned* rb_solved;
+    unsigned* rb_hot;
     int64_t part_stride = 0;
     unsigned long long* tmax;
     void* E = nullptr;
@@ -1544,6 +1609,8 @@ struct qdfn_ctx {
     int64_t xbuf = 0;                // elements per shared-memory x buffer
     int64_t xd_stride = 0, rb_stride = 0;
     int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
+    int pair_solve = 1;              // lane-pair solves in the overlapped phase (QDFN_PAIR_SOLVE=0: one lane)
+    int rb_ordered = 1;              // high-velocity row blocks first (QDFN_RB_ORDER=0: index order)
     int c_spec = 8;                  // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS)
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
@@ -1604,7 +1671,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.tld = c->tld; p.knd = c->knd; p.instab = c->instab; p.flag = c->flag; p.sw = c->sw;
     p.sw_n = c->sw_n; p.accel_n = c->accel_n;
     p.part_s = c->part_s; p.part_n = c->part_n; p.part_stride = c->part_stride;
-    p.spec_ctr = c->spec_ctr; p.rb_solved = c->rb_solved; p.c_spec = c->c_spec;
+    p.spec_ctr = c->spec_ctr; p.rb_solved = c->rb_solved; p.c_spec = c->c_spec; p.rb_hot = c->rb_hot;
     p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
@@ -1614,6 +1681,8 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.rb_done = c->rb_done;
     p.tmax = c->tmax;
     p.hold_cap = c->hold_cap;
+    p.pair_solve = c->pair_solve;
+    p.rb_ordered = c->rb_ordered;
     p.n_rb = c->ld > 0 ? (c->N + c->ld - 1) / c->ld : 0;
     p.h = c->hops;
     p.budget_ns = budget_ns;
@@ -1684,6 +1753,8 @@ int configure_launch(qdfn_ctx* c) {
         int64_t tiles_per_sm = 4;
         if (const char* e = std::getenv("QDFN_TILES_PER_SM")) tiles_per_sm = std::max(1, std::min(64, std::atoi(e)));
         if (const char* e = std::getenv("QDFN_SOLVE_HOLD")) c->hold_cap = std::max(1, std::min(64, std::atoi(e)));
+        if (const char* e = std::getenv("QDFN_PAIR_SOLVE")) c->pair_solve = std::atoi(e) != 0 ? 1 : 0;
+        if (const char* e = std::getenv("QDFN_RB_ORDER")) c->rb_ordered = std::atoi(e) != 0 ? 1 : 0;
         if (const char* e = std::getenv("QDFN_SPEC_COLS")) c->c_spec = std::max(0, std::min(64, std::atoi(e)));
         int64_t want_chunks = std::max<int64_t>(1, (tiles_per_sm * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
@@ -1799,9 +1870,10 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
         c->bar_gen = reinterpret_cast<unsigned*>(ctrl + 2);
     }
     A(prof, kCounters); A(tile_ctr, 3); A(spec_ctr, 3);
-    // per-step counters, two sets used by alternate steps (one is reset while the other runs)
+    // per-step counters, three sets used by steps in turn (a step uses one, streams
+    // ahead into the next, and resets the one after)
     c->rb_stride = (N + kOpThreads - 1) / kOpThreads;   // row blocks have >= kOpThreads rows
-    A(solve_ctr, 3); A(tmax, 12); A(rb_done, 3 * (size_t)c->rb_stride); A(rb_solved, 3 * (size_t)c->rb_stride);
+    A(solve_ctr, 3); A(tmax, 12); A(rb_done, 3 * (size_t)c->rb_stride); A(rb_solved, 3 * (size_t)c->rb_stride); A(rb_hot, 3 * (size_t)c->rb_stride);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0

@@ -117,6 +117,39 @@ __device__ __forceinline__ double evolution(double ThetaOld, double Dt, double V
 }
 
 // Semi-analytic harmonic-oscillator update with a secant iteration on V.
+//
+// As in the low-velocity solver below, an iteration's first evaluation is at
+// the V of the previous iteration's update, whose Theta and Friction =
+// mu0 + a ln(V/V0) + b ln(V0 Theta/Dc) are the first terms of that evaluation
+// (same operations on the same operands), so they are reused.
+#define QDFN_RESET() do { V = p.VOld; Theta = p.ThetaOld; Friction = p.FrictionOld; Disp = p.DispOld; } while (0)
+// one evaluation of the oscillator map at Vx, given Theta and the friction
+// prefix there: the V it returns
+#define QDFN_OSC_V(Vx, Fpre)                                                            \
+    ([&]() {                                                                            \
+        const double Fr_ = (Fpre) + eta / p.sigma * (Vx) - p.dtau / p.sigma;            \
+        const double F_ = p.TLD + (p.tau0 - Fr_ * p.sigma) / p.K_Self;                  \
+        const double D_ = (p.DispOld - F_) * cO + (p.VOld / p.Omega) * sO + F_;         \
+        return div_by(D_ - p.DispOld, Rdt) * 2 - p.VOld;                                \
+    }())
+#define QDFN_FPRE(Vx, Tx, errx) \
+    (p.Friction0 + p.a * jlog((Vx) / kV0, errx) + p.b * jlog(div_by((Tx) * kV0, Rdc), errx))
+// :87-134 -- both the negative and the NaN branch halve Dt; below Dt = 1e-5
+// they also mark Instability = 4 (the V<0 branch) or do so after printing
+// (the NaN branch)
+#define QDFN_HV_NEG()                                                         \
+    do {                                                                      \
+        if (Dt > 1e-5) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }  \
+        else { Dt = Dt / 2; Instab = 4; QDFN_RESET(); maxDiff = 0; FLAG = 0; } \
+    } while (0)
+#define QDFN_HV_CAP()                                                         \
+    do {                                                                      \
+        if (Iteration % 100 == 0) {                                           \
+            if (Dt < 1e-5) { crit = crit * 10; Instab = 2; }                  \
+            else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }        \
+        }                                                                     \
+    } while (0)
+
 __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
                                 int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
@@ -130,49 +163,38 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
     const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
     // divisors fixed for the solve (Dt only changes on the way out of the loop)
     const Recip Rdc = recip(p.Dc), Rdt = recip(Dt);
-#define QDFN_RESET() do { V = p.VOld; Theta = p.ThetaOld; Friction = p.FrictionOld; Disp = p.DispOld; } while (0)
+    bool at_v = false;   // Theta and Friction are the update's values at V
     while (maxDiff > crit) {
         Iteration++;
         if (Iteration > kHighVIterCap) { err = QDFN_ERR_NO_CONVERGE; break; }
         const double VTest = V;
-        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
-        if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-        double Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err) +
-                    eta / p.sigma * V - p.dtau / p.sigma;
-        double F = p.TLD + (p.tau0 - Fr * p.sigma) / p.K_Self;
-        Disp = (p.DispOld - F) * cO + (p.VOld / p.Omega) * sO + F;
-        V = div_by(Disp - p.DispOld, Rdt) * 2 - p.VOld;
+        if (!at_v) {
+            Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
+            if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
+            Friction = QDFN_FPRE(V, Theta, err);
+        }
+        V = QDFN_OSC_V(VTest, Friction);
         const double FOriginal = VTest - V;
         V = VTest + DV;
         const double VTest2 = V;
         Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
         if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-        Fr = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err) +
-             eta / p.sigma * V - p.dtau / p.sigma;
-        F = p.TLD + (p.tau0 - Fr * p.sigma) / p.K_Self;
-        Disp = (p.DispOld - F) * cO + (p.VOld / p.Omega) * sO + F;
-        V = div_by(Disp - p.DispOld, Rdt) * 2 - p.VOld;
+        V = QDFN_OSC_V(VTest2, QDFN_FPRE(VTest2, Theta, err));
         const double FUpdated = VTest2 - V;
         V = VTest - FOriginal * DV / (FUpdated - FOriginal);
         if (V < 0 || isnan(V)) {
-            // :87-134 -- both the negative and the NaN branch halve Dt; below
-            // Dt = 1e-5 they also mark Instability = 4 (the V<0 branch) or do so
-            // after printing (the NaN branch)
-            if (Dt > 1e-5) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
-            else { Dt = Dt / 2; Instab = 4; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
+            QDFN_HV_NEG();
         } else {
             Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
             Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, err);
             if (Theta < 0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
-            Friction = p.Friction0 + p.a * jlog(V / kV0, err) + p.b * jlog(div_by(Theta * kV0, Rdc), err);
+            Friction = QDFN_FPRE(V, Theta, err);
             maxDiff = fabs(VTest / V - 1);
             Instab = 0;
         }
-        if (Iteration % 100 == 0) {
-            if (Dt < 1e-5) { crit = crit * 10; Instab = 2; }
-            else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
-        }
+        QDFN_HV_CAP();
         if (err) break;
+        at_v = true;
     }
     PatchOut o;
     o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
@@ -180,22 +202,135 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
     return o;
 }
 
+// One lane pair per patch (the even lane's result is the solve's), both lanes
+// running the same instructions on different points: iteration 1 evaluates
+// at V (even) and V + DV (odd); after each secant step the even lane evaluates
+// at the new V -- its Theta and friction prefix are the update's -- and the
+// odd lane at the new V + DV, the next iteration's two evaluations.  Errors
+// count where the reference loop raises them: the update's (evolution law,
+// friction logarithms) only when the update runs (V >= 0, not NaN); the
+// second evaluation's only when the first passed.
+__device__ PatchOut solve_highv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+                                     int& err) {
+    int FLAG = 1, Instab = 0, Iteration = 0;
+    double maxDiff = 10, crit = kConv;
+    const double DV = p.VOld / 100;
+    double V = p.VOld / 1e10, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
+    if (V < 0) V = 1e-100;
+    const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
+    const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
+    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt);
+    const int lane = threadIdx.x & 31, base = lane & ~1;
+    const bool odd = (lane & 1) != 0;
+    const unsigned pmask = 3u << base;
+    // one evaluation at Vh: Theta, the friction prefix and the residual
+    double Th, Fp, FVh;
+    int eh, tc;
+    auto evaluate = [&](double Vh) {
+        eh = 0;
+        Fp = 0;
+        FVh = 0;
+        Th = evolution(p.ThetaOld, Dt, Vh, Rdc, alpha, p.sigma, p.sigma_old, p.b, 1, dr, skip, eh);
+        tc = Th < 0 ? 1 : 0;
+        if (!tc) {
+            Fp = QDFN_FPRE(Vh, Th, eh);
+            FVh = Vh - QDFN_OSC_V(Vh, Fp);
+        }
+    };
+    Iteration = 1;   // 1 <= kHighVIterCap
+    double VTest = V;
+    evaluate(odd ? VTest + DV : VTest);
+    int fail0 = __shfl_sync(pmask, tc, base), fail1 = __shfl_sync(pmask, tc, base + 1);
+    int err0 = __shfl_sync(pmask, eh, base), err1 = __shfl_sync(pmask, eh, base + 1);
+    double FO = __shfl_sync(pmask, FVh, base), FU = __shfl_sync(pmask, FVh, base + 1);
+    for (;;) {
+        if (err0) err = err0;
+        if (fail0) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
+        if (err1) err = err1;
+        if (fail1) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
+        V = VTest - FO * DV / (FU - FO);
+        if (V < 0 || isnan(V)) {
+            QDFN_HV_NEG();
+            QDFN_HV_CAP();
+            break;   // maxDiff = 0 ends the loop (after the error check, which would too)
+        }
+        Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
+        evaluate(odd ? V + DV : V);
+        const int tcode = __shfl_sync(pmask, tc, base);
+        const int erru = __shfl_sync(pmask, eh, base);
+        const int f1 = __shfl_sync(pmask, tc, base + 1), e1 = __shfl_sync(pmask, eh, base + 1);
+        const double FOn = __shfl_sync(pmask, FVh, base), FUn = __shfl_sync(pmask, FVh, base + 1);
+        // the even lane's evaluation is the update at V
+        Theta = Th;
+        if (erru) err = erru;
+        if (tcode) { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; break; }
+        Friction = Fp;
+        maxDiff = fabs(VTest / V - 1);
+        Instab = 0;
+        QDFN_HV_CAP();
+        if (err) break;
+        if (!(maxDiff > crit)) break;
+        Iteration++;
+        if (Iteration > kHighVIterCap) { err = QDFN_ERR_NO_CONVERGE; break; }
+        VTest = V;
+        fail0 = 0; err0 = 0;   // the update's values: its errors are counted already
+        fail1 = f1; err1 = e1;
+        FO = FOn; FU = FUn;
+    }
+    PatchOut o;
+    o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
+    o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
+    return o;
+}
+#undef QDFN_OSC_V
+#undef QDFN_FPRE
+#undef QDFN_HV_NEG
+#undef QDFN_HV_CAP
+
 // Implicit trapezoidal update with a secant iteration on V and the friction
 // inversion V = V0 exp((mu - mu0 - b ln(V0 theta/Dc))/a), all in FP64.
 //
-// kPair: the solve of one patch runs on a lane pair (lanes 2k, 2k+1 of the
-// warp, same inputs).  The two evaluations of the secant step -- at V and at
-// V + DV -- are independent, so lane 2k evaluates at V and lane 2k+1 at V + DV,
-// and they exchange the residuals; everything else runs on both lanes alike.
-// The arithmetic and every branch decision are those of the one-lane solve
-// (an evaluation's error counts only when the one before it passed, as in the
-// sequential order), so both return the same result.  A lone warp issues one
-// FP64 instruction per ~70 cycles on this part, so halving the dependent chain
-// of an iteration matters where few warps are left to run (the last row
-// blocks of a step).
-template <bool kPair>
-__device__ PatchOut solve_lowv_t(const PatchIn& p, double Dt, double eta, double alpha, int dr,
-                                 double SwitchV, int& err) {
+// One iteration of the reference loop: evaluate the residual at VTest = V and
+// at V + DV (each: Accel, Theta, Disp, Friction, then the friction inversion),
+// take the secant step to a new V, then update Accel, Disp, Theta, Friction and
+// maxDiff at the new V.  The next iteration's first evaluation is at exactly
+// that V, so its Accel, Theta, Disp and Friction are the values the update just
+// formed (same operations on the same operands; with --fmad=false no
+// contraction can differ), and they passed the update's Theta checks -- only
+// the friction inversion is new.  Both solvers below reuse them and return what
+// the reference loop returns, bit for bit.
+#define QDFN_FAIL_A()                                                    \
+    do {                                                                   \
+        if (Dt < SwitchV) { Instab = 3; QDFN_RESET(); FLAG = 0; }          \
+        else if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }                  \
+        else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }         \
+    } while (0)
+#define QDFN_FRICTION(Vx, Dx, Ax) \
+    (inv_sig * (p.K_Self * (p.TLD - (Dx)) + p.tau0 - eta * (Vx) + p.dtau - p.Mass * (Ax)))
+#define QDFN_VEL(Fx, Tx, errx) \
+    (kV0 * exp(div_by((Fx) - p.Friction0 - p.b * jlog(div_by(kV0 * (Tx), Rdc), errx), Ra)))
+// Theta came out NaN in the update (Solvers :283-301)
+#define QDFN_THETA_NAN()                                                                     \
+    do {                                                                                     \
+        if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }                                         \
+        else if (Dt < 1e-3) {                                                                \
+            if (p.VOld < 1e-7) {                                                             \
+                V = 0; Theta = p.ThetaOld + Dt; Friction = p.FrictionOld; Disp = p.DispOld;  \
+                maxDiff = 0; FLAG = 1;                                                       \
+            } else { Instab = 3; QDFN_RESET(); FLAG = 0; }                                   \
+        } else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }                         \
+    } while (0)
+// every 200 iterations (Solvers :309-318); always leaves the loop
+#define QDFN_ITER_CAP()                                              \
+    do {                                                             \
+        if (Dt < 1e-4) { Instab = 3; QDFN_RESET(); FLAG = 0; }       \
+        else if (Dt < 1e1) { crit = crit * 2; }                      \
+        else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }   \
+    } while (0)
+
+// One lane per patch.
+__device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+                               double SwitchV, int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;
     double V = p.VOld, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
@@ -205,63 +340,28 @@ __device__ PatchOut solve_lowv_t(const PatchIn& p, double Dt, double eta, double
     // 1e-10 is the correctly rounded reciprocal of 1e10 (both are 10^-10 rounded)
     const Recip Rdc = recip(p.Dc), Rdt = recip(Dt), Ra = recip(p.a);
     const Recip R1e10 = {1e10, 1e-10, true};
-#define QDFN_FAIL_A()                                                    \
-    do {                                                                   \
-        if (Dt < SwitchV) { Instab = 3; QDFN_RESET(); FLAG = 0; }          \
-        else if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }                  \
-        else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }         \
-    } while (0)
-#define QDFN_FRICTION(Vx, Dx, Ax) \
-    (inv_sig * (p.K_Self * (p.TLD - (Dx)) + p.tau0 - eta * (Vx) + p.dtau - p.Mass * (Ax)))
-    const int lane = threadIdx.x & 31, base = lane & ~1;
-    const unsigned pmask = 3u << base;
-    (void)lane; (void)pmask;
+    double Accel = 0;
+    bool at_v = false;   // Accel, Theta, Disp, Friction are the update's values at V
     while (maxDiff > crit) {
         Iteration++;
         const double VTest = V;
         const double DV = div_by(VTest, R1e10);
-        double FV, FV_DeV, VTest2, Accel;
-        if constexpr (!kPair) {
+        if (!at_v) {
             Accel = div_by(V - p.VOld, Rdt);
             Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
             if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
             Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
             Friction = QDFN_FRICTION(V, Disp, Accel);
-            double Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
-            FV = VTest - Vel;
-            V = V + DV;
-            VTest2 = V;
-            Accel = div_by(V - p.VOld, Rdt);
-            Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
-            if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
-            Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
-            Friction = QDFN_FRICTION(V, Disp, Accel);
-            Vel = kV0 * exp(div_by(Friction - p.Friction0 - p.b * jlog(div_by(kV0 * Theta, Rdc), err), Ra));
-            FV_DeV = VTest2 - Vel;
-        } else {
-            // this lane's evaluation point: V (even lane) or V + DV (odd lane)
-            const double Vh = (lane & 1) ? VTest + DV : VTest;
-            int errh = 0;
-            const double Ah = div_by(Vh - p.VOld, Rdt);
-            const double Th = evolution(p.ThetaOld, Dt, Vh, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, errh);
-            const int failh = (Th < 0 || isnan(Th)) ? 1 : 0;
-            double FVh = 0;
-            if (!failh) {
-                const double Dh = p.DispOld + (p.VOld + Vh) / 2 * Dt;
-                const double Frh = QDFN_FRICTION(Vh, Dh, Ah);
-                const double Velh = kV0 * exp(div_by(Frh - p.Friction0 - p.b * jlog(div_by(kV0 * Th, Rdc), errh), Ra));
-                FVh = Vh - Velh;
-            }
-            const int fail0 = __shfl_sync(pmask, failh, base), fail1 = __shfl_sync(pmask, failh, base + 1);
-            const int err0 = __shfl_sync(pmask, errh, base), err1 = __shfl_sync(pmask, errh, base + 1);
-            FV = __shfl_sync(pmask, FVh, base);
-            FV_DeV = __shfl_sync(pmask, FVh, base + 1);
-            if (err0) err = err0;
-            if (fail0) { QDFN_FAIL_A(); break; }
-            if (err1) err = err1;        // the second evaluation runs only after the first passed
-            if (fail1) { QDFN_FAIL_A(); break; }
-            VTest2 = VTest + DV;
         }
+        const double FV = VTest - QDFN_VEL(Friction, Theta, err);
+        V = V + DV;
+        const double VTest2 = V;
+        Accel = div_by(V - p.VOld, Rdt);
+        Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
+        if (Theta < 0 || isnan(Theta)) { QDFN_FAIL_A(); break; }
+        Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
+        Friction = QDFN_FRICTION(V, Disp, Accel);
+        const double FV_DeV = VTest2 - QDFN_VEL(Friction, Theta, err);
         V = VTest - FV * DV / (FV_DeV - FV);
         if (dr != 1 && V < 0)
             V = exp(jlog(VTest, err) - FV * jlog(VTest2 / VTest, err) / (FV_DeV - FV));
@@ -269,38 +369,121 @@ __device__ PatchOut solve_lowv_t(const PatchIn& p, double Dt, double eta, double
         Disp = p.DispOld + (p.VOld + V) / 2 * Dt;
         Theta = evolution(p.ThetaOld, Dt, V, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, err);
         if (Theta < 0) { QDFN_FAIL_A(); break; }
-        if (isnan(Theta)) {
-            if (p.VOld == 0) { QDFN_RESET(); FLAG = 1; }
-            else if (Dt < 1e-3) {
-                if (p.VOld < 1e-7) {
-                    V = 0; Theta = p.ThetaOld + Dt; Friction = p.FrictionOld; Disp = p.DispOld;
-                    maxDiff = 0; FLAG = 1;
-                } else { Instab = 3; QDFN_RESET(); FLAG = 0; }
-            } else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
-            break;
-        }
+        if (isnan(Theta)) { QDFN_THETA_NAN(); break; }
         Friction = QDFN_FRICTION(V, Disp, Accel);
         maxDiff = fabs(VTest / V - 1);
-        if (Iteration % 200 == 0) {
-            if (Dt < 1e-4) { Instab = 3; QDFN_RESET(); FLAG = 0; break; }
-            else if (Dt < 1e1) { crit = crit * 2; }
-            else { Dt = Dt / 2; QDFN_RESET(); maxDiff = 0; FLAG = 0; }
-            break;
-        }
+        if (Iteration % 200 == 0) { QDFN_ITER_CAP(); break; }
         if (err) break;
+        at_v = true;
     }
-#undef QDFN_FAIL_A
-#undef QDFN_FRICTION
-#undef QDFN_RESET
     PatchOut o;
     o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
     o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
     return o;
 }
-__device__ __forceinline__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
-                                               double SwitchV, int& err) {
-    return solve_lowv_t<false>(p, Dt, eta, alpha, dr, SwitchV, err);
+
+// One lane pair per patch (lanes 2k, 2k+1 of the warp, same inputs; the even
+// lane's result is the solve's).  Both lanes run the same instructions on
+// different points -- an evaluation each -- so the warp never splits:
+//   iteration 1: the even lane evaluates at V, the odd lane at V + DV;
+//   every iteration: exchange the outcomes, take the secant step to the new V
+//     (the same arithmetic on both lanes), then evaluate again: the even lane
+//     at the new V -- its Accel, Disp, Theta and Friction are the update's, and
+//     its friction inversion is the next iteration's first evaluation -- and
+//     the odd lane at the new V + V/1e10, the next iteration's second;
+//   exchange, then the update's decisions (Theta < 0, NaN, the 200-iteration
+//     rule, errors, convergence) on the same values on both lanes.
+// So an iteration's dependent chain is one evaluation and the secant step,
+// instead of two evaluations' worth.  The next iteration's evaluations are
+// formed before the decision to run it and dropped if the loop ends.  Errors
+// count where the reference loop raises them: the update's evolution-law error
+// at once, an evaluation's when its iteration runs (the second only when the
+// first passed).  A lone warp issues one FP64 instruction per ~70 cycles on
+// this part, so the chain sets the solve time where few warps are left to run
+// (the last row blocks of a step).
+__device__ PatchOut solve_lowv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+                                    double SwitchV, int& err) {
+    int FLAG = 1, Instab = 0, Iteration = 0;
+    double maxDiff = 10, crit = kConv;
+    double V = p.VOld, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
+    const double inv_sig = 1 / p.sigma;
+    const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
+    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt), Ra = recip(p.a);
+    const Recip R1e10 = {1e10, 1e-10, true};
+    const int lane = threadIdx.x & 31, base = lane & ~1;
+    const bool odd = (lane & 1) != 0;
+    const unsigned pmask = 3u << base;
+    // one evaluation at Vh: Theta, Disp and -- if Theta passed -- Friction and
+    // the residual; the evolution law's and the inversion's errors apart
+    double Th, Dh, Frh, FVh;
+    int errT, errV, tc;
+    auto evaluate = [&](double Vh) {
+        errT = 0;
+        errV = 0;
+        FVh = 0;
+        Frh = 0;
+        const double Ah = div_by(Vh - p.VOld, Rdt);
+        Th = evolution(p.ThetaOld, Dt, Vh, Rdc, alpha, p.sigma, p.sigma_old, p.b, 0, dr, skip, errT);
+        Dh = p.DispOld + (p.VOld + Vh) / 2 * Dt;
+        tc = Th < 0 ? 1 : (isnan(Th) ? 2 : 0);
+        if (tc == 0) {
+            Frh = QDFN_FRICTION(Vh, Dh, Ah);
+            FVh = Vh - QDFN_VEL(Frh, Th, errV);
+        }
+    };
+    Iteration = 1;
+    double VTest = V;
+    double DV = div_by(VTest, R1e10);
+    evaluate(odd ? VTest + DV : VTest);
+    int fail0 = __shfl_sync(pmask, tc != 0 ? 1 : 0, base), fail1 = __shfl_sync(pmask, tc != 0 ? 1 : 0, base + 1);
+    int err0 = __shfl_sync(pmask, errT ? errT : errV, base), err1 = __shfl_sync(pmask, errT ? errT : errV, base + 1);
+    double FV = __shfl_sync(pmask, FVh, base), FV_DeV = __shfl_sync(pmask, FVh, base + 1);
+    for (;;) {
+        if (err0) err = err0;
+        if (fail0) { QDFN_FAIL_A(); break; }
+        if (err1) err = err1;        // the second evaluation runs only after the first passed
+        if (fail1) { QDFN_FAIL_A(); break; }
+        const double VTest2 = VTest + DV;
+        V = VTest - FV * DV / (FV_DeV - FV);
+        if (dr != 1 && V < 0)
+            V = exp(jlog(VTest, err) - FV * jlog(VTest2 / VTest, err) / (FV_DeV - FV));
+        const double DVn = div_by(V, R1e10);
+        evaluate(odd ? V + DVn : V);
+        maxDiff = fabs(VTest / V - 1);
+        // the even lane's evaluation is the update at V
+        Theta = Th;
+        Disp = Dh;
+        if (tc == 0) Friction = Frh;
+        const int tcode = __shfl_sync(pmask, tc, base);
+        const int erru = __shfl_sync(pmask, errT, base);
+        const int e0 = __shfl_sync(pmask, errV, base);
+        const int f1 = __shfl_sync(pmask, tc != 0 ? 1 : 0, base + 1);
+        const int e1 = __shfl_sync(pmask, errT ? errT : errV, base + 1);
+        const double FVn = __shfl_sync(pmask, FVh, base), FV_DeVn = __shfl_sync(pmask, FVh, base + 1);
+        if (erru) err = erru;
+        if (tcode == 1) { QDFN_FAIL_A(); break; }
+        if (tcode == 2) { QDFN_THETA_NAN(); break; }
+        if (Iteration % 200 == 0) { QDFN_ITER_CAP(); break; }
+        if (err) break;
+        if (!(maxDiff > crit)) break;
+        Iteration++;
+        VTest = V;
+        DV = DVn;
+        fail0 = 0; err0 = e0;
+        fail1 = f1; err1 = e1;
+        FV = FVn; FV_DeV = FV_DeVn;
+    }
+    PatchOut o;
+    o.V = V; o.Friction = Friction; o.Disp = Disp; o.Theta = Theta; o.Dt = Dt;
+    o.Instab = Instab; o.Flag = FLAG; o.Iterations = Iteration;
+    return o;
 }
+#undef QDFN_FAIL_A
+#undef QDFN_FRICTION
+#undef QDFN_VEL
+#undef QDFN_THETA_NAN
+#undef QDFN_ITER_CAP
+#undef QDFN_RESET
 
 // InterpolateFromStressChange for one patch column.
 __device__ __forceinline__ void interp_ext(int64_t nt, const double* __restrict__ t,

@@ -146,7 +146,7 @@ class Simulation:
                 "lowv_solves", "lowv_iterations", "highv_solves", "highv_iterations",
                 "ns_solve_own", "ns_solve_wait", "ns_operator_warps", "ns_solver_warps",
                 "ns_operator_warps_slowest", "ns_solver_warps_slowest",
-                "ns_chunk_solve_longest", "ns_chunk_partials_longest")
+                "ns_chunk_solve_longest", "ns_last_row_block")
         return {k: int(out[i]) for i, k in enumerate(keys)}
 
     # -- state --------------------------------------------------------------
