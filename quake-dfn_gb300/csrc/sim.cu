@@ -34,6 +34,11 @@ namespace qdfn {
 namespace {
 
 constexpr int kSimThreads = 512;
+// per-step counter sets in rotation: step s uses set s, streams the next
+// step's early tiles into set s+1 and resets set s+2 (mod kSets), whose last
+// reader -- step s-2's early-tile producers, which may run into the start of
+// step s-1 -- has passed a grid barrier since
+constexpr int kSets = 4;
 constexpr int kGranule = 8;                 // operator bytes per thread and source column
 constexpr int kMaxInst = 4;
 constexpr int kRedSlots = 16;               // doubles per (CTA, instance) partial
@@ -115,8 +120,8 @@ struct SimParams {
     // barrier + reductions
     unsigned *bar_count, *bar_gen;
     double* red;                     // [2][nblocks][R][kRedSlots]
-    // per-step counters, three sets used by steps s, s+1, s+2 (mod 3): [3], and
-    // rb_done / rb_solved [3][rb_stride]
+    // per-step counters, kSets sets used by steps in turn (mod kSets): [kSets],
+    // and rb_done / rb_solved / rb_hot [kSets][rb_stride]
     unsigned long long* tile_ctr;    // dynamic tile counter of the dense operator
     unsigned long long* spec_ctr;    // tiles of the step streamed ahead during the step before
     unsigned* rb_solved;             // dense: solved row chunks per row block
@@ -131,8 +136,8 @@ struct SimParams {
     int pair_solve;                  // overlapped phase: one lane pair per patch (else the even lanes alone)
     int rb_ordered;                  // FP32/BF16 dense: row blocks with high-velocity patches first
     int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
-    unsigned long long* tmax;        // [3][4] per-step max over blocks of (operator end, solver end,
-                                     // chunk ready->solved, chunk partial sums), ns
+    unsigned long long* tmax;        // [kSets][4] per-step max over blocks of (operator end, solver end,
+                                     // chunk ready->solved, last row block complete), ns
 };
 
 // bounded grid barrier; returns false on timeout, or as soon as another block
@@ -258,6 +263,49 @@ constexpr int kOpWarps = 8;                                     // operator role
 constexpr int kOpThreads = kOpWarps * 32;
 constexpr int kProducerWarp = kSimThreads / 32 - 1;             // lane 0 fills the stage ring
 constexpr int kStages = 3;
+// FP32/BF16 steps that stream ahead: the solver warps [kOpWarps, kProducerWarp)
+// run the step's first reduction pass and its grid barrier on their own
+// (named barrier 1) while the operator warps and the producer finish the early
+// tiles; everyone meets afterwards
+constexpr int kSolverWarps = kProducerWarp - kOpWarps;
+constexpr int kSolverThreads = kSolverWarps * 32;
+__device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kSolverThreads) : "memory"); }
+// early-tile counter: closed (no further claims) once the step's solves are in
+constexpr unsigned long long kSpecClosed = 1ull << 62;
+
+// The same barrier for the solver warps of each block alone (named barrier 1;
+// thread kOpThreads arrives for the block).  Every solver thread gets the same
+// result.
+__device__ bool grid_barrier_solvers(const SimParams& p, uint64_t deadline_ns) {
+    __shared__ int s_ok;
+    solver_sync();
+    if (threadIdx.x == kOpThreads) {
+        volatile unsigned* gen = p.bar_gen;
+        const unsigned my_gen = *gen;
+        __threadfence();
+        const unsigned prev = atomicAdd(p.bar_count, 1u);
+        int ok = 1;
+        if (prev == gridDim.x - 1) {
+            atomicExch(p.bar_count, 0u);
+            __threadfence();
+            atomicAdd((unsigned*)p.bar_gen, 1u);
+        } else {
+            while (*gen == my_gen) {
+                if (globaltimer_ns() > deadline_ns + 2000000000ull || *(volatile int*)p.gerr != 0) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (!ok) atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
+        s_ok = ok;
+    }
+    solver_sync();
+    return s_ok != 0;
+}
+
 constexpr int kColsPerStage = 16;
 constexpr int kFoldStages = 32 / kColsPerStage;                 // FP32 sums span 32 columns
 constexpr int kSegBytes = kOpThreads * kGranule;                // one column of a row block, 2 KB
@@ -563,13 +611,20 @@ __device__ void rb_order(const SimParams& p, int set, unsigned short* order) {
     const int lane = threadIdx.x & 31;
     const int nrb = (int)p.n_rb, s0 = (int)min(p.rb_small0, (int64_t)nrb);
     const unsigned* hot = p.rb_hot + (int64_t)set * p.rb_stride;
+    // the flags of row blocks lane + 32 j, loaded at once (nrb <= kMaxOrder)
+    unsigned bits = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxOrder / 32; ++j) {
+        const int b = lane + 32 * j;
+        if (b < nrb && __ldcg(hot + b) != 0u) bits |= 1u << j;
+    }
     int pos = 0;
     for (int grp = 0; grp < 2; ++grp) {
         const int lo = grp ? s0 : 0, hi = grp ? nrb : s0;
         for (int want = 1; want >= 0; --want)
-            for (int b0 = lo; b0 < hi; b0 += 32) {
-                const int b = b0 + lane;
-                const bool take = b < hi && ((__ldcg(hot + b) != 0u) == (want == 1));
+            for (int j = lo / 32; j * 32 < hi; ++j) {
+                const int b = lane + 32 * j;
+                const bool take = b >= lo && b < hi && (((bits >> j) & 1u) == (unsigned)want);
                 const unsigned m = __ballot_sync(0xffffffffu, take);
                 if (take) order[pos + __popc(m & ((1u << lane) - 1u))] = (unsigned short)b;
                 pos += __popc(m);
@@ -590,8 +645,8 @@ __device__ __forceinline__ void spec_shape(const SimParams& p, int64_t nrb, int6
 // row-block completion and solved-chunk counts, diagnostics maxima and, with
 // `hot`, the row-block order flags).  Called by every thread of one block, with
 // no other block using the set.
-__device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, bool hot) {
-    if (threadIdx.x == 0) {
+__device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, bool hot, int tid, int nthr) {
+    if (tid == 0) {
         atomicExch(p.tile_ctr + s, 0ull);
         atomicExch(p.spec_ctr + s, 0ull);
         atomicExch(p.solve_ctr + s, 0ull);
@@ -599,12 +654,27 @@ __device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, boo
     unsigned* a = p.rb_done + (int64_t)s * p.rb_stride;
     unsigned* b = p.rb_solved + (int64_t)s * p.rb_stride;
     unsigned* h = p.rb_hot + (int64_t)s * p.rb_stride;
-    for (int64_t k = threadIdx.x; k < p.n_rb; k += blockDim.x) {
+    for (int64_t k = tid; k < p.n_rb; k += nthr) {
         a[k] = 0u;
         b[k] = 0u;
         if (hot) h[k] = 0u;
     }
-    if (threadIdx.x < 4) p.tmax[s * 4 + threadIdx.x] = 0ull;
+    if (tid < 4) p.tmax[s * 4 + tid] = 0ull;
+}
+
+// Claim the next early tile: its index, or -1 once n are claimed or the
+// counter is closed (the step's solves are in).  A compare-and-swap, so a
+// closed counter keeps the number of tiles claimed; bounded -- a tile left
+// unclaimed is streamed by its own step.
+__device__ __forceinline__ long long claim_spec(unsigned long long* ctr, int64_t n) {
+    unsigned long long v = ld_acquire_u64(ctr);
+    for (int k = 0; k < 256; ++k) {
+        if ((v & kSpecClosed) != 0 || (long long)v >= (long long)n) return -1;
+        const unsigned long long w = atomicCAS(ctr, v, v + 1);
+        if (w == v) return (long long)v;
+        v = w;
+    }
+    return -1;
 }
 
 // Producer (one lane): fill the next stage of the ring -- the next stage of the
@@ -646,8 +716,8 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
                 break;
             }
             // the next step (fphase 1)
-            const long long u = (long long)atomicAdd(p.spec_ctr + sc.set_next, 1ull);
-            if (u >= n_spec) { pp.fphase = 2; continue; }
+            const long long u = claim_spec(p.spec_ctr + sc.set_next, n_spec);
+            if (u < 0) { pp.fphase = 2; continue; }
             const int64_t rb = u % nrb_reg, c = u / nrb_reg;
             const long long t = rb * p.nchunk + c;
             // its x chunk: the slip of patches [j0, j0 + L), solved in this step
@@ -987,8 +1057,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (blockIdx.x == 0 && HM) atomicExch(p.tile_ctr, 0ull);
         }
         if (!HM && blockIdx.x == 0) {   // the counter sets of steps 0 and 1
-            reset_counter_set(p, 0, true);
-            reset_counter_set(p, 1, true);
+            reset_counter_set(p, 0, true, threadIdx.x, blockDim.x);
+            reset_counter_set(p, 1, true, threadIdx.x, blockDim.x);
             __threadfence();
         }
         if (!grid_barrier(p, deadline)) return;
@@ -1016,8 +1086,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (stop) break;
         }
         const int par = s_par;             // which buffer holds the current state
-        const int cpar = (int)(it % 3);    // which counter set this step uses (the next step: +1 mod 3)
-        const int cnext = (int)((it + 1) % 3);
+        const int cpar = (int)(it % kSets);   // which counter set this step uses
+        const int cnext = (int)((it + 1) % kSets);
         if (threadIdx.x < R) s_done[threadIdx.x] = 0;
         // FP32/BF16 dense: the step's row-block order (rows that start on the
         // high-velocity solver first), from flags the previous step's solves set
@@ -1178,14 +1248,20 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             __shared__ int s_fused_fail;
             __shared__ int s_held;       // row chunks this block holds (grabbed, not yet solved)
             __shared__ unsigned long long s_t_solve;
-            if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; s_held = 0; }
+            __shared__ int s_p3_abort;   // the solver warps' grid barrier gave up
+            if (threadIdx.x == 0) { s_fused_fail = 0; s_t_solve = 0; s_held = 0; s_p3_abort = 0; }
             __syncthreads();
             const uint64_t t_f0 = globaltimer_ns();
             sc.t0 = t_f0;
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            // a step that streams ahead: the operator warps and the producer
+            // stream to the end (early tiles included) and do not solve; the
+            // solver warps then run the first reduction pass on their own
+            const bool dec = sc.spec != 0;
             bool solve = true;
             if (warp < kOpWarps) {
                 if (!dense_matvec<M, R>(p, pipe, xs, sc)) { s_fused_fail = 1; solve = false; }
+                if (dec) solve = false;
                 if (threadIdx.x == 0) {
                     const uint64_t d = globaltimer_ns() - t_f0;
                     s_tm[6] += d;
@@ -1197,11 +1273,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     // this step's tiles already streamed during the step before
                     int64_t nrb_reg, n_spec;
                     spec_shape(p, p.n_rb, &nrb_reg, &n_spec);
-                    sc.spec_done = (long long)min((int64_t)ld_acquire_u64(p.spec_ctr + cpar), n_spec);
+                    sc.spec_done =
+                        (long long)min((int64_t)(ld_acquire_u64(p.spec_ctr + cpar) & ~kSpecClosed), n_spec);
                     pok = produce_tiles<M, R>(p, pipe, xs, sc) ? 1 : 0;
                 }
                 pok = __shfl_sync(0xffffffffu, pok, 0);
                 if (!pok) { s_fused_fail = 1; solve = false; }
+                if (dec) solve = false;
             }
             if (solve) {
                 constexpr int64_t rpb = (int64_t)kOpThreads * M::VEC;   // operator row block
@@ -1278,18 +1356,98 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 }
                 if (lane == 0) atomicMax(&s_t_solve, (unsigned long long)(globaltimer_ns() - t_f0));
             }
+            if (dec && warp >= kOpWarps && warp < kProducerWarp) {
+                // The step's first reduction pass, by the solver warps alone,
+                // while the operator warps finish the early tiles they hold.
+                // Every solver thread runs the same barriers (named barrier 1)
+                // and takes the same branches; none returns before the block
+                // meets again below.
+                const int gt = threadIdx.x - kOpThreads;
+                solver_sync();   // the block's solves are in (s_red complete)
+                if (gt == 0) s_tm[11] = globaltimer_ns();
+                if (blockIdx.x == 0) {
+                    // the counter set two steps ahead (its last users have passed
+                    // a grid barrier since), and no more early tiles for the next
+                    // step: their number is final once every block has arrived
+                    reset_counter_set(p, (int)((it + 2) % kSets), true, gt, kSolverThreads);
+                    if (gt == 0) atomicOr(p.spec_ctr + cnext, kSpecClosed);
+                    __threadfence();
+                }
+                if (gt == 0) {
+                    const double late = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
+                    for (int r = 0; r < R; ++r) {
+                        double* sl = red_slot(phase, blockIdx.x, r);
+                        for (int k = 0; k < 8; ++k) sl[k] = ord_val(s_red[r][k]);
+                        sl[8] = late;
+                    }
+                }
+                const uint64_t t_items = gt == 0 ? globaltimer_ns() : 0;
+                if (!grid_barrier_solvers(p, deadline)) {
+                    if (gt == 0) s_p3_abort = 1;
+                } else {
+                    if (gt == 0) {
+                        const uint64_t t = globaltimer_ns();
+                        s_tm[4] += t_items - s_tm[11];
+                        s_tm[5] += t - t_items;
+                        s_tm[11] = t;
+                        if (blockIdx.x == 0 && it > 0) {   // the previous step's maxima are complete
+                            const int ps = (int)((it + kSets - 1) % kSets);
+                            s_tm[8] += __ldcg(p.tmax + ps * 4);
+                            s_tm[9] += __ldcg(p.tmax + ps * 4 + 1);
+                            s_tm[12] += __ldcg(p.tmax + ps * 4 + 2);
+                            s_tm[13] += __ldcg(p.tmax + ps * 4 + 3);
+                        }
+                    }
+                    const int r = gt >> 5;
+                    if (r < R) {
+                        const int ops[9] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
+                        double f[9];
+                        grid_fields<9>(p.red + (int64_t)(phase & 1) * gridDim.x * R * kRedSlots, gridDim.x, R, r,
+                                       ops, f);
+                        const double mflag = f[0], mdt = f[1], any4 = f[2], err = f[3];
+                        if ((threadIdx.x & 31) == 0) {
+                            if (f[8] != 0) s_stop = 1;
+                            if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
+                            else if (mflag == 0) {
+                                s_dt[r] = any4 != 0 ? 1e-3 : mdt;
+                            } else {
+                                s_dt[r] = mdt;   // Main_D :262 Dt = minimum(Dt_All)
+                                s_done[r] = 1;
+                                bool empty;
+                                s_dtn[r] = next_dt(p, f[4], f[5], f[6], f[7], mdt, &empty);
+                                if (empty && s_fail[r] == 0) s_fail[r] = QDFN_ERR_EMPTY;
+                            }
+                        }
+                    }
+                }
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_tm[7] += s_t_solve;
                 atomicMax(p.tmax + cpar * 4 + 1, s_t_solve);
             }
-            if (s_fused_fail) return;
+            if (s_fused_fail || s_p3_abort) return;
         }
         lap(1);
         // ---------------------------------------------------------- P3
-        if (threadIdx.x == 0) { s_iter = 0; s_tm[11] = globaltimer_ns(); }
+        // pass 0 already ran in the solver warps when the step streamed ahead
+        const bool pass0_done = !HM && sizeof(X) == 4 && sc.spec != 0;
+        if (pass0_done) { phase++; n_iter++; }
+        if (threadIdx.x == 0) {
+            s_iter = pass0_done ? 1 : 0;
+            if (!pass0_done) s_tm[11] = globaltimer_ns();
+        }
         __syncthreads();
-        for (;;) {
+        bool more = true;
+        if (pass0_done) {
+            int all = 1;
+            for (int r = 0; r < R; ++r) all &= s_done[r];
+            more = !all;
+            // a retry discards the next step's early tiles: every block must
+            // have finished those it holds before their counters are reset
+            if (more && !grid_barrier(p, deadline)) return;
+        }
+        while (more) {
             const int first = (s_iter == 0);
             if (HM || sizeof(X) == 8 || !first) {   // FP32/BF16 dense pass 0 ran alongside the operator
                 if (!first) {
@@ -1308,14 +1466,14 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 }
             }
             if (!HM && blockIdx.x == 0 && (first || s_iter == 1)) {
-                // pass 0: reset the counter set of the step after next (its last
-                // use was the previous step, which every block has left; the
-                // next step's early tiles will use it during the next step).
+                // pass 0: reset the counter set two steps ahead (its last users
+                // have passed a grid barrier since; the next step's early tiles
+                // will use it).
                 // First retry pass: this step's slip changes, so the next step's
                 // early tiles are discarded -- their counters start again (the
                 // order flags stay: the retry's solves add to them, and the
                 // order only decides when work is taken, not its result)
-                reset_counter_set(p, first ? (int)((it + 2) % 3) : cnext, first);
+                reset_counter_set(p, first ? (int)((it + 2) % kSets) : cnext, first, threadIdx.x, blockDim.x);
                 __threadfence();
             }
             __syncthreads();
@@ -1337,10 +1495,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     s_tm[11] = t;
                 }
                 if (!HM && first && blockIdx.x == 0 && threadIdx.x == 0) {   // every block has stored its max
-                    s_tm[8] += __ldcg(p.tmax + cpar * 4);
-                    s_tm[9] += __ldcg(p.tmax + cpar * 4 + 1);
-                    s_tm[12] += __ldcg(p.tmax + cpar * 4 + 2);
-                    s_tm[13] += __ldcg(p.tmax + cpar * 4 + 3);
+                    // (a step that streamed ahead had its maxima read by the step after)
+                    const bool prev_ahead = it > 0 && sizeof(X) == 4 && p.c_spec > 0;
+                    for (int k = prev_ahead ? 0 : 1; k < 2; ++k) {
+                        const int ss = k == 0 ? (int)((it + kSets - 1) % kSets) : cpar;
+                        s_tm[8] += __ldcg(p.tmax + ss * 4);
+                        s_tm[9] += __ldcg(p.tmax + ss * 4 + 1);
+                        s_tm[12] += __ldcg(p.tmax + ss * 4 + 2);
+                        s_tm[13] += __ldcg(p.tmax + ss * 4 + 3);
+                    }
                 }
             }
             if ((threadIdx.x >> 5) < R) {
@@ -1869,11 +2032,12 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
         c->bar_count = reinterpret_cast<unsigned*>(ctrl + 1);
         c->bar_gen = reinterpret_cast<unsigned*>(ctrl + 2);
     }
-    A(prof, kCounters); A(tile_ctr, 3); A(spec_ctr, 3);
-    // per-step counters, three sets used by steps in turn (a step uses one, streams
-    // ahead into the next, and resets the one after)
+    A(prof, kCounters); A(tile_ctr, kSets); A(spec_ctr, kSets);
+    // per-step counters, kSets sets used by steps in turn (a step uses one, streams
+    // ahead into the next, and resets the one two ahead)
     c->rb_stride = (N + kOpThreads - 1) / kOpThreads;   // row blocks have >= kOpThreads rows
-    A(solve_ctr, 3); A(tmax, 12); A(rb_done, 3 * (size_t)c->rb_stride); A(rb_solved, 3 * (size_t)c->rb_stride); A(rb_hot, 3 * (size_t)c->rb_stride);
+    A(solve_ctr, kSets); A(tmax, 4 * kSets); A(rb_done, kSets * (size_t)c->rb_stride);
+    A(rb_solved, kSets * (size_t)c->rb_stride); A(rb_hot, kSets * (size_t)c->rb_stride);
 #undef A
     if (rc) { delete c; return rc; }
     // host-side initialisation (Main_D :41-131): padded instances replicate instance 0
