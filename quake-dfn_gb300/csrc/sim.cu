@@ -1774,7 +1774,7 @@ struct qdfn_ctx {
     int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
     int pair_solve = 1;              // lane-pair solves in the overlapped phase (QDFN_PAIR_SOLVE=0: one lane)
     int rb_ordered = 1;              // high-velocity row blocks first (QDFN_RB_ORDER=0: index order)
-    int c_spec = 8;                  // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS)
+    int c_spec = 16;                 // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS)
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
