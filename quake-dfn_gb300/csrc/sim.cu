@@ -699,18 +699,26 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
     if (pp.ftile == -2 || (pp.ftile >= 0 && pp.fq >= pp.fnst)) {
         int64_t nrb_reg, n_spec;
         spec_shape(p, nrb, &nrb_reg, &n_spec);
-        const int64_t cs = min(p.c_spec, p.nchunk);
         pp.ftile = -1;
         while (pp.fphase < 2) {
             if (pp.fphase == 0) {            // this step
-                long long t = (long long)atomicAdd(p.tile_ctr + sc.set, 1ull);
-                if (t >= ntiles) { pp.fphase = (sc.spec && n_spec > 0) ? 1 : 2; continue; }
-                TileGeo g = tile_geo(p, nrb, t);
-                if (sc.order) {   // the g.rb-th row block of the step's order (same tile shape)
-                    t = tile_index(p, nrb, sc.order[g.rb], g.c);
-                    g = tile_geo(p, nrb, t);
+                // the step's own tiles: every tile but the sc.spec_done early
+                // ones (column-major prefix over the full-width row blocks:
+                // chunks c < cfull of each, and chunk cfull of row blocks < rem),
+                // row block after row block in the step's order
+                const long long k = (long long)atomicAdd(p.tile_ctr + sc.set, 1ull);
+                if (k >= ntiles - sc.spec_done) { pp.fphase = (sc.spec && n_spec > 0) ? 1 : 2; continue; }
+                const int64_t cfull = nrb_reg > 0 ? sc.spec_done / nrb_reg : 0;
+                const int64_t rem = nrb_reg > 0 ? sc.spec_done % nrb_reg : 0;
+                long long t = -1, left = k;
+                for (int64_t pos = 0; pos < nrb; ++pos) {
+                    const int64_t rb = sc.order ? (int64_t)sc.order[pos] : pos;
+                    const int64_t c0 = rb < nrb_reg ? cfull + (rb < rem ? 1 : 0) : 0;
+                    const int64_t cnt = (rb < nrb_reg ? p.nchunk : p.nchunk2) - c0;
+                    if (left < cnt) { t = tile_index(p, nrb, rb, c0 + left); break; }
+                    left -= cnt;
                 }
-                if (g.rb < nrb_reg && g.c < cs && (int64_t)g.c * nrb_reg + g.rb < sc.spec_done) continue;
+                if (t < 0) { pp.fphase = (sc.spec && n_spec > 0) ? 1 : 2; continue; }   // (not reached)
                 pp.ftile = t;
                 pp.fnext = 0;
                 break;
