@@ -37,7 +37,7 @@ def loaded_network(qdfn_mod):
     return prob, Ks, Kn, ext
 
 
-def _run(net, env, nsteps, chunk):
+def _run(net, env, nsteps, chunk, precision):
     """States after every `chunk` steps, with `env` set while the context is
     configured (the schedule settings are read then)."""
     from qdfn import simulate
@@ -46,7 +46,7 @@ def _run(net, env, nsteps, chunk):
     try:
         os.environ.update({k: str(v) for k, v in env.items()})
         sim = simulate.Simulation(prob, n_inst=2)
-        sim.set_dense(Ks, Kn, "fp32")
+        sim.set_dense(Ks, Kn, precision)
         sim.set_blocks(16)
     finally:
         for k, v in old.items():
@@ -71,10 +71,11 @@ def _same(a, b):
                 assert np.array_equal(sa[r][k], sb[r][k], equal_nan=True), k
 
 
-def test_early_tiles_and_lane_pairs_change_no_bit(qdfn_mod, loaded_network):
+@pytest.mark.parametrize("precision", ["fp32", "bf16x2"])
+def test_early_tiles_and_lane_pairs_change_no_bit(qdfn_mod, loaded_network, precision):
     nsteps, chunk = 400, 100
     ref, cnt = _run(loaded_network, {"QDFN_SPEC_COLS": 0, "QDFN_PAIR_SOLVE": 0, "QDFN_RB_ORDER": 0},
-                    nsteps, chunk)
+                    nsteps, chunk, precision)
     # the horizon reaches retried steps (each discards the next step's early
     # tiles) and the high-velocity solver
     assert cnt["solve_passes"] > cnt["steps"] and cnt["highv_solves"] > 0, cnt
@@ -82,5 +83,5 @@ def test_early_tiles_and_lane_pairs_change_no_bit(qdfn_mod, loaded_network):
                 {"QDFN_SPEC_COLS": 16, "QDFN_PAIR_SOLVE": 1, "QDFN_RB_ORDER": 1},    # every column chunk early
                 {"QDFN_SPEC_COLS": 0, "QDFN_PAIR_SOLVE": 1, "QDFN_RB_ORDER": 0},
                 {"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 0, "QDFN_RB_ORDER": 1}):
-        got, _ = _run(loaded_network, env, nsteps, chunk)
+        got, _ = _run(loaded_network, env, nsteps, chunk, precision)
         _same(ref, got)
