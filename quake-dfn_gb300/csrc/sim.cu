@@ -231,7 +231,8 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
     unsigned long long acc[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = ord_key(ops[k] == 0 ? -INFINITY : INFINITY);
-    for (int b = lane; b < nblk; b += 32) {
+#pragma unroll 2
+    for (int b = lane; b < nblk; b += 32) {   // (two blocks' slots in flight per lane)
         const double* s = slots_base + ((int64_t)b * R + r) * kRedSlots;
 #pragma unroll
         for (int k = 0; k < K; ++k) acc[k] = key_op(ops[k], acc[k], ord_key(__ldcg(s + k)));
@@ -1099,9 +1100,15 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         if (threadIdx.x < R) s_done[threadIdx.x] = 0;
         // FP32/BF16 dense: the step's row-block order (rows that start on the
         // high-velocity solver first), from flags the previous step's solves set
-        __shared__ unsigned short s_order[kMaxOrder];
+        // (double-buffered: the solver warps of the step before may have formed
+        // this one's order, and the early-tile count, in its first pass)
+        __shared__ unsigned short s_order[2][kMaxOrder];
+        __shared__ long long s_next_valid;       // step whose order/early count is precomputed
+        __shared__ long long s_next_spec_done;
+        if (it == 0 && threadIdx.x == 0) s_next_valid = -1;   // (read after the barrier below)
         const bool use_order = !HM && sizeof(X) == 4 && p.rb_ordered && p.n_rb <= kMaxOrder;
-        if (use_order && threadIdx.x < 32) rb_order(p, cpar, s_order);
+        const bool pre = it > 0 && s_next_valid == it;
+        if (use_order && !pre && threadIdx.x < 32) rb_order(p, cpar, s_order[it & 1]);
         red_init();
         __syncthreads();
         const X* xdc = reinterpret_cast<const X*>(p.xd) + (size_t)par * p.xd_stride;
@@ -1111,7 +1118,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         StepCtx sc{cpar, cnext, (int)(it & 1), xdc,
                    reinterpret_cast<const X*>(p.xd) + (size_t)(par ^ 1) * p.xd_stride, 0,
                    (!HM && sizeof(X) == 4 && p.c_spec > 0 && it + 1 < nsteps) ? 1 : 0};
-        sc.order = use_order ? s_order : nullptr;
+        sc.order = use_order ? s_order[it & 1] : nullptr;
+        if (pre) sc.spec_done = s_next_spec_done;
         // one (instance r, patch i) item of a solve pass; pass 0 of a step also
         // forms the row's operator products.  pair: the item runs on a lane
         // pair (lanes 2k, 2k+1, both called with it); the even lane writes the
@@ -1281,8 +1289,9 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     // this step's tiles already streamed during the step before
                     int64_t nrb_reg, n_spec;
                     spec_shape(p, p.n_rb, &nrb_reg, &n_spec);
-                    sc.spec_done =
-                        (long long)min((int64_t)(ld_acquire_u64(p.spec_ctr + cpar) & ~kSpecClosed), n_spec);
+                    if (!pre)
+                        sc.spec_done =
+                            (long long)min((int64_t)(ld_acquire_u64(p.spec_ctr + cpar) & ~kSpecClosed), n_spec);
                     pok = produce_tiles<M, R>(p, pipe, xs, sc) ? 1 : 0;
                 }
                 pok = __shfl_sync(0xffffffffu, pok, 0);
@@ -1407,6 +1416,18 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                         }
                     }
                     const int r = gt >> 5;
+                    if (r == kSolverWarps - 1 && r >= R) {
+                        // the next step's row order and early-tile count: final
+                        // now unless this step retries (then they are formed again)
+                        if (use_order) rb_order(p, cnext, s_order[(it + 1) & 1]);
+                        if ((threadIdx.x & 31) == 0) {
+                            int64_t nrb_reg, n_spec;
+                            spec_shape(p, p.n_rb, &nrb_reg, &n_spec);
+                            s_next_spec_done = (long long)min(
+                                (int64_t)(ld_acquire_u64(p.spec_ctr + cnext) & ~kSpecClosed), n_spec);
+                            s_next_valid = it + 1;
+                        }
+                    }
                     if (r < R) {
                         const int ops[9] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
                         double f[9];
@@ -1453,6 +1474,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             more = !all;
             // a retry discards the next step's early tiles: every block must
             // have finished those it holds before their counters are reset
+            if (more && threadIdx.x == 0) s_next_valid = -1;
             if (more && !grid_barrier(p, deadline)) return;
         }
         while (more) {
