@@ -136,6 +136,7 @@ struct SimParams {
     int pair_solve;                  // overlapped phase: one lane pair per patch (else the even lanes alone)
     int rb_ordered;                  // FP32/BF16 dense: row blocks with high-velocity patches first
     int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
+    int spec_stop;                   // no early-tile claims once this many blocks reached the step's barrier
     unsigned long long* tmax;        // [kSets][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, last row block complete), ns
 };
@@ -276,8 +277,10 @@ constexpr unsigned long long kSpecClosed = 1ull << 62;
 
 // The same barrier for the solver warps of each block alone (named barrier 1;
 // thread kOpThreads arrives for the block).  Every solver thread gets the same
-// result.
-__device__ bool grid_barrier_solvers(const SimParams& p, uint64_t deadline_ns) {
+// result.  The last block to arrive closes the early-tile counter `close`
+// before it releases the others, so the number of early tiles is final for
+// every block that leaves the barrier.
+__device__ bool grid_barrier_solvers(const SimParams& p, uint64_t deadline_ns, unsigned long long* close) {
     __shared__ int s_ok;
     solver_sync();
     if (threadIdx.x == kOpThreads) {
@@ -287,6 +290,7 @@ __device__ bool grid_barrier_solvers(const SimParams& p, uint64_t deadline_ns) {
         const unsigned prev = atomicAdd(p.bar_count, 1u);
         int ok = 1;
         if (prev == gridDim.x - 1) {
+            atomicOr(close, kSpecClosed);
             atomicExch(p.bar_count, 0u);
             __threadfence();
             atomicAdd((unsigned*)p.bar_gen, 1u);
@@ -663,11 +667,14 @@ __device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, boo
     if (tid < 4) p.tmax[s * 4 + tid] = 0ull;
 }
 
-// Claim the next early tile: its index, or -1 once n are claimed or the
-// counter is closed (the step's solves are in).  A compare-and-swap, so a
-// closed counter keeps the number of tiles claimed; bounded -- a tile left
+// Claim the next early tile: its index, or -1 once n are claimed, the counter
+// is closed (every block's solves are in), or `stop` blocks have arrived at the
+// step's barrier -- a tile claimed later would still be streaming when the
+// step is decided and hold its block's next step back.  A compare-and-swap, so
+// a closed counter keeps the number of tiles claimed; bounded -- a tile left
 // unclaimed is streamed by its own step.
-__device__ __forceinline__ long long claim_spec(unsigned long long* ctr, int64_t n) {
+__device__ __forceinline__ long long claim_spec(const SimParams& p, unsigned long long* ctr, int64_t n) {
+    if (*(volatile unsigned*)p.bar_count >= (unsigned)p.spec_stop) return -1;
     unsigned long long v = ld_acquire_u64(ctr);
     for (int k = 0; k < 256; ++k) {
         if ((v & kSpecClosed) != 0 || (long long)v >= (long long)n) return -1;
@@ -725,7 +732,7 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
                 break;
             }
             // the next step (fphase 1)
-            const long long u = claim_spec(p.spec_ctr + sc.set_next, n_spec);
+            const long long u = claim_spec(p, p.spec_ctr + sc.set_next, n_spec);
             if (u < 0) { pp.fphase = 2; continue; }
             const int64_t rb = u % nrb_reg, c = u / nrb_reg;
             const long long t = rb * p.nchunk + c;
@@ -1384,10 +1391,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 if (gt == 0) s_tm[11] = globaltimer_ns();
                 if (blockIdx.x == 0) {
                     // the counter set two steps ahead (its last users have passed
-                    // a grid barrier since), and no more early tiles for the next
-                    // step: their number is final once every block has arrived
+                    // a grid barrier since)
                     reset_counter_set(p, (int)((it + 2) % kSets), true, gt, kSolverThreads);
-                    if (gt == 0) atomicOr(p.spec_ctr + cnext, kSpecClosed);
                     __threadfence();
                 }
                 if (gt == 0) {
@@ -1399,7 +1404,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     }
                 }
                 const uint64_t t_items = gt == 0 ? globaltimer_ns() : 0;
-                if (!grid_barrier_solvers(p, deadline)) {
+                if (!grid_barrier_solvers(p, deadline, p.spec_ctr + cnext)) {
                     if (gt == 0) s_p3_abort = 1;
                 } else {
                     if (gt == 0) {
@@ -1804,7 +1809,9 @@ struct qdfn_ctx {
     int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
     int pair_solve = 1;              // lane-pair solves in the overlapped phase (QDFN_PAIR_SOLVE=0: one lane)
     int rb_ordered = 1;              // high-velocity row blocks first (QDFN_RB_ORDER=0: index order)
-    int c_spec = 16;                 // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS)
+    int c_spec = 64;                 // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS;
+                                     // at most the chunks of a full-width row block, so 64: all of them)
+    int spec_stop_pct = 100;         // % of blocks at the barrier that ends early-tile claims (QDFN_SPEC_STOP)
     hmat::Ops hops{};
     std::vector<void*> hbufs;       // H-matrix device buffers
     size_t smem = 0;
@@ -1865,6 +1872,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.sw_n = c->sw_n; p.accel_n = c->accel_n;
     p.part_s = c->part_s; p.part_n = c->part_n; p.part_stride = c->part_stride;
     p.spec_ctr = c->spec_ctr; p.rb_solved = c->rb_solved; p.c_spec = c->c_spec; p.rb_hot = c->rb_hot;
+    p.spec_stop = std::max(1, (c->nblocks * c->spec_stop_pct + 99) / 100);
     p.T = c->T; p.dt = c->dt; p.step = c->step; p.nrec = c->nrec; p.status = c->status;
     p.hT = c->hT; p.hDt = c->hDt; p.hV = c->hV; p.hD = c->hD; p.hth = c->hth; p.hs = c->hs;
     p.bar_count = c->bar_count; p.bar_gen = c->bar_gen; p.red = c->red; p.gerr = c->gerr;
@@ -1949,6 +1957,7 @@ int configure_launch(qdfn_ctx* c) {
         if (const char* e = std::getenv("QDFN_PAIR_SOLVE")) c->pair_solve = std::atoi(e) != 0 ? 1 : 0;
         if (const char* e = std::getenv("QDFN_RB_ORDER")) c->rb_ordered = std::atoi(e) != 0 ? 1 : 0;
         if (const char* e = std::getenv("QDFN_SPEC_COLS")) c->c_spec = std::max(0, std::min(64, std::atoi(e)));
+        if (const char* e = std::getenv("QDFN_SPEC_STOP")) c->spec_stop_pct = std::max(1, std::min(100, std::atoi(e)));
         int64_t want_chunks = std::max<int64_t>(1, (tiles_per_sm * sms + nrb - 1) / nrb);
         int64_t clen = (c->N + want_chunks - 1) / want_chunks;
         // two x buffers (R x chunk x elem each) share the 227 KB with the 192 KB stage ring
