@@ -81,6 +81,7 @@ struct SimParams {
     int64_t record_step, max_records;
     // per [R][N] constants
     const double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega;
+    const double *ra, *rDc;          // 1/a and 1/Dc, correctly rounded (fixed for a run)
     const double* kself;             // [N]
     const unsigned char* unstable;   // [R][N]
     const int* has_unstable;         // [R]
@@ -990,6 +991,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
     // reductions of the current one; s_dta: the last accepted Dt (what the
     // host keeps, and the next launch's controller starts from)
     __shared__ double s_T[kMaxInst], s_dt[kMaxInst], s_dtn[kMaxInst], s_dta[kMaxInst];
+    __shared__ double s_rdt[kMaxInst];   // 1/s_dt, correctly rounded, formed before each solve pass
     __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
     __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop, s_par;
     __shared__ int s_iter;
@@ -1116,6 +1118,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
         const bool use_order = !HM && sizeof(X) == 4 && p.rb_ordered && p.n_rb <= kMaxOrder;
         const bool pre = it > 0 && s_next_valid == it;
         if (use_order && !pre && threadIdx.x < 32) rb_order(p, cpar, s_order[it & 1]);
+        if (threadIdx.x >= 32 && threadIdx.x < 32 + R) s_rdt[threadIdx.x - 32] = 1.0 / s_dt[threadIdx.x - 32];
         red_init();
         __syncthreads();
         const X* xdc = reinterpret_cast<const X*>(p.xd) + (size_t)par * p.xd_stride;
@@ -1176,6 +1179,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                 pin.ThetaOld = QDFN_CUR(theta, thn)[q];
                 pin.VOld = VOld; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
                 pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
+                pin.rDc = p.rDc[q]; pin.ra = p.ra[q]; pin.rDt = s_rdt[r];
                 pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
                 pin.dtau = dss; pin.sigma_old = QDFN_CUR(sig_old, sn)[q]; pin.tau0 = p.tau0[q];
                 int err = 0;
@@ -1487,6 +1491,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (HM || sizeof(X) == 8 || !first) {   // FP32/BF16 dense pass 0 ran alongside the operator
                 if (!first) {
                     red_init();
+                    if (threadIdx.x < R) s_rdt[threadIdx.x] = 1.0 / s_dt[threadIdx.x];
                     __syncthreads();
                 }
                 // every CTA takes an equal contiguous range of (instance, patch)
@@ -1775,6 +1780,7 @@ struct qdfn_ctx {
     // device buffers
     std::vector<void*> allocs;
     double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega, *kself;
+    double *ra = nullptr, *rDc = nullptr;
     unsigned char* unstable;
     int* has_unstable;
     double *V, *D, *theta, *fric, *accel, *sig_old, *Vn, *Dn, *thn, *fn, *sn, *dtall, *tld, *knd;
@@ -1860,6 +1866,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.alpha_evo = c->prob.alpha_evo;
     p.record_step = c->prob.record_step; p.max_records = c->prob.max_records;
     p.a = c->a; p.b = c->b; p.Dc = c->Dc; p.F0 = c->F0; p.tau0 = c->tau0; p.sigma0 = c->sigma0;
+    p.ra = c->ra; p.rDc = c->rDc;
     p.Vconst = c->Vconst; p.mass = c->mass; p.omega = c->omega; p.kself = c->kself;
     p.unstable = c->unstable; p.has_unstable = c->has_unstable;
     p.n_ext = c->n_ext; p.ext_t = c->ext_t; p.ext_n = c->ext_n; p.ext_s = c->ext_s; p.ext_p = c->ext_p;
@@ -2045,6 +2052,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     int rc = 0;
 #define A(ptr, n) if (!rc) rc = c->dalloc(&c->ptr, n)
     A(a, RN); A(b, RN); A(Dc, RN); A(F0, RN); A(tau0, RN); A(sigma0, RN); A(Vconst, RN);
+    A(ra, RN); A(rDc, RN);
     A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
     // the six host-visible state fields in one block, in the order of the
     // state-transfer calls, so that contiguous host buffers move in one copy
@@ -2102,10 +2110,15 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
             if (hun[q]) hhas[r] = 1;
         }
     }
+    // the solvers divide by a and Dc through their reciprocals: IEEE 1/x,
+    // correctly rounded here as on the device
+    std::vector<double> hra(RN), hrDc(RN);
+    for (size_t q = 0; q < RN; ++q) { hra[q] = 1.0 / ha[q]; hrDc[q] = 1.0 / hDc[q]; }
     std::vector<double> ones(Rk, 1.0), zeros(Rk, 0.0);
     std::vector<int64_t> z64(Rk, 0);
     std::vector<int> z32(Rk, 0);
     if ((rc = h2d(c->a, ha.data(), RN * 8)) || (rc = h2d(c->b, hb.data(), RN * 8)) ||
+        (rc = h2d(c->ra, hra.data(), RN * 8)) || (rc = h2d(c->rDc, hrDc.data(), RN * 8)) ||
         (rc = h2d(c->Dc, hDc.data(), RN * 8)) || (rc = h2d(c->F0, hF0.data(), RN * 8)) ||
         (rc = h2d(c->tau0, htau0.data(), RN * 8)) || (rc = h2d(c->sigma0, hs0.data(), RN * 8)) ||
         (rc = h2d(c->Vconst, hVc.data(), RN * 8)) || (rc = h2d(c->mass, hm.data(), RN * 8)) ||

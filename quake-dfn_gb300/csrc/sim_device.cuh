@@ -26,6 +26,7 @@ constexpr int kHighVIterCap = 40000;      // tolerance*10 per 100 its reaches In
 struct PatchIn {
     double DispOld, FrictionOld, ThetaOld, VOld, Friction0, a, b, Dc, K_Self, Omega, Mass;
     double sigma, TLD, dtau, sigma_old, tau0;
+    double ra, rDc, rDt;   // 1/a, 1/Dc, 1/Dt correctly rounded (Dt: the step the solve starts from)
 };
 struct PatchOut {
     double V, Friction, Disp, Theta, Dt;
@@ -68,6 +69,14 @@ __device__ __forceinline__ Recip recip(double d) {
     Recip r;
     r.d = d;
     r.y = 1.0 / d;
+    r.ok = in_safe_range(exp_field(d));
+    return r;
+}
+// The same from a reciprocal formed earlier (y = 1/d correctly rounded).
+__device__ __forceinline__ Recip recip_pre(double d, double y) {
+    Recip r;
+    r.d = d;
+    r.y = y;
     r.ok = in_safe_range(exp_field(d));
     return r;
 }
@@ -162,7 +171,7 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
     // constant for every iteration that reaches them, so once is the same
     const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
     // divisors fixed for the solve (Dt only changes on the way out of the loop)
-    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt);
+    const Recip Rdc = recip_pre(p.Dc, p.rDc), Rdt = recip_pre(Dt, p.rDt);
     bool at_v = false;   // Theta and Friction are the update's values at V
     while (maxDiff > crit) {
         Iteration++;
@@ -219,7 +228,7 @@ __device__ PatchOut solve_highv_pair(const PatchIn& p, double Dt, double eta, do
     if (V < 0) V = 1e-100;
     const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
     const double cO = cos(p.Omega * Dt), sO = sin(p.Omega * Dt);
-    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt);
+    const Recip Rdc = recip_pre(p.Dc, p.rDc), Rdt = recip_pre(Dt, p.rDt);
     const int lane = threadIdx.x & 31, base = lane & ~1;
     const bool odd = (lane & 1) != 0;
     const unsigned pmask = 3u << base;
@@ -338,7 +347,7 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
     const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
     // divisors fixed for the solve (Dt only changes on the way out of the loop);
     // 1e-10 is the correctly rounded reciprocal of 1e10 (both are 10^-10 rounded)
-    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt), Ra = recip(p.a);
+    const Recip Rdc = recip_pre(p.Dc, p.rDc), Rdt = recip_pre(Dt, p.rDt), Ra = recip_pre(p.a, p.ra);
     const Recip R1e10 = {1e10, 1e-10, true};
     double Accel = 0;
     bool at_v = false;   // Accel, Theta, Disp, Friction are the update's values at V
@@ -408,7 +417,7 @@ __device__ PatchOut solve_lowv_pair(const PatchIn& p, double Dt, double eta, dou
     double V = p.VOld, Disp = p.DispOld, Friction = p.FrictionOld, Theta = p.ThetaOld;
     const double inv_sig = 1 / p.sigma;
     const bool skip = dr == 1 && alpha_term_zero(alpha, Dt, p.sigma, p.sigma_old, p.b);
-    const Recip Rdc = recip(p.Dc), Rdt = recip(Dt), Ra = recip(p.a);
+    const Recip Rdc = recip_pre(p.Dc, p.rDc), Rdt = recip_pre(Dt, p.rDt), Ra = recip_pre(p.a, p.ra);
     const Recip R1e10 = {1e10, 1e-10, true};
     const int lane = threadIdx.x & 31, base = lane & ~1;
     const bool odd = (lane & 1) != 0;
