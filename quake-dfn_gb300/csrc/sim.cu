@@ -1225,7 +1225,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             // the next step's Accel, solver switch and time-control statistics
             // (Main_D :265-319 then :162-201) -- final once the step is accepted,
             // since an accepted pass keeps its Dt
-            const double A = (Vnew - VOld) / Dt;
+            const double A = sim::div_by(Vnew - VOld, sim::recip_pre(Dt, s_rdt[r]));   // (Vnew - VOld) / Dt
             QDFN_NXT(accel, accel_n)[q] = A;
             QDFN_NXT(sw, sw_n)[q] = Vnew > p.switch_v ? 1 : 0;
             if constexpr (!HM) {   // the next step streams and solves this row block early
