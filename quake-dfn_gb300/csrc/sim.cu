@@ -1972,13 +1972,17 @@ int configure_launch(qdfn_ctx* c) {
         clen = (std::min<int64_t>(std::max<int64_t>(clen, 64), std::min<int64_t>(2048, cmax)) + 7) / 8 * 8;
         c->chunk_len = clen;
         c->nchunk = (int)((c->N + clen - 1) / clen);
-        // narrower tiles (1/tail_div of the width; QDFN_TAIL_DIV, default 2) for
-        // the row blocks of the last two waves of tiles
-        int64_t tail_div = 2;
-        if (const char* e = std::getenv("QDFN_TAIL_DIV")) tail_div = std::max(1, std::min(16, std::atoi(e)));
-        c->chunk_len2 = std::max<int64_t>(8, ((clen + tail_div - 1) / tail_div + 7) / 8 * 8);
+        // the row blocks of the last two waves of tiles are streamed by their own
+        // step only, in tiles of 1/tail_div of the width (QDFN_TAIL_DIV; 1 by
+        // default: full width; 0: no such row blocks, every row block open to
+        // the next step's early tiles)
+        int64_t tail_div = 1;
+        if (const char* e = std::getenv("QDFN_TAIL_DIV")) tail_div = std::max(0, std::min(16, std::atoi(e)));
+        const int64_t td = std::max<int64_t>(1, tail_div);
+        c->chunk_len2 = std::max<int64_t>(8, ((clen + td - 1) / td + 7) / 8 * 8);
         c->nchunk2 = (int)((c->N + c->chunk_len2 - 1) / c->chunk_len2);
-        const int64_t nsmall = std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
+        const int64_t nsmall =
+            tail_div == 0 ? 0 : std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
         c->rb_small0 = nrb - nsmall;
         // one x buffer: the chunk's columns rounded up to 4 (bulk copies move
         // multiples of 16 bytes), in 128-byte units
