@@ -1981,8 +1981,10 @@ int configure_launch(qdfn_ctx* c) {
         const int64_t td = std::max<int64_t>(1, tail_div);
         c->chunk_len2 = std::max<int64_t>(8, ((clen + td - 1) / td + 7) / 8 * 8);
         c->nchunk2 = (int)((c->N + c->chunk_len2 - 1) / c->chunk_len2);
+        int64_t waves = 2;   // (QDFN_TAIL_WAVES)
+        if (const char* e = std::getenv("QDFN_TAIL_WAVES")) waves = std::max(1, std::min(16, std::atoi(e)));
         const int64_t nsmall =
-            tail_div == 0 ? 0 : std::min<int64_t>(nrb, (2LL * sms + c->nchunk2 - 1) / c->nchunk2);
+            tail_div == 0 ? 0 : std::min<int64_t>(nrb, (waves * sms + c->nchunk2 - 1) / c->nchunk2);
         c->rb_small0 = nrb - nsmall;
         // one x buffer: the chunk's columns rounded up to 4 (bulk copies move
         // multiples of 16 bytes), in 128-byte units
