@@ -370,8 +370,6 @@ __device__ __forceinline__ void fence_proxy_async() {
 __device__ __forceinline__ void fence_proxy_async_global() {
     asm volatile("fence.proxy.async.global;" ::: "memory");
 }
-// barrier of the operator role alone (named barrier 1, warps [0, kOpWarps))
-__device__ __forceinline__ void op_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kOpThreads) : "memory"); }
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* ptr) {
     unsigned long long v;
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ptr) : "memory");
