@@ -3,16 +3,20 @@
 // One cooperative launch advances every instance of a context by `nsteps` time
 // steps.  Per step (scripts/Functions_RSFDFN3DMain_D.jl:146-322):
 //   P1  solver switch (VOld > SwitchV) and the time-step control reductions
-//       (max V and min |V/Accel| over the unstable patches, :163-187)
-//   --  grid barrier; every CTA reduces the per-CTA partials itself, so all CTAs
-//       hold identical step scalars without another round trip
+//       (max V and min |V/Accel| over the unstable patches, :163-187) -- once
+//       per launch; afterwards folded into each step's solve pass
 //   P2  elastic operator: one pass over the shear (K_ij/K_ii) and normal
 //       matrices computes both products for all instances at once
-//   --  grid barrier
 //   P3  per-patch secant solves (SolveOneTimeStep, Functions_Solvers.jl:334),
 //       then the retry decision (:240-253) -- repeated until every instance
 //       accepts its step
-//   P4  history record, T += Dt, Accel, state rotation (:265-319)
+//   P4  history record, T += Dt, Accel, state buffers swap (:265-319)
+// With the dense FP32/BF16 operator, P2 and P3's first pass overlap within each
+// block (operator warps stream tiles, solver warps solve each row block as its
+// tiles complete), the operator warps go on to the next step's tiles whose
+// slip is already solved, and the solver warps run P3's reductions and grid
+// barrier on their own meanwhile.  Every CTA reduces the per-CTA partials
+// itself, so all CTAs hold identical step scalars without another round trip.
 // Grid barriers are a counter/generation pair with a bounded wait on
 // %globaltimer: a wait that outlives the deadline sets QDFN_ERR_TIMEOUT and the
 // kernel returns.  The launch is cooperative, so all CTAs are co-resident.
@@ -587,7 +591,7 @@ __device__ __forceinline__ TileGeo tile_geo(const SimParams& p, int64_t nrb, int
 
 // What the producer and the operator warps need to know about a step.
 struct StepCtx {
-    int set, set_next;        // counter sets of this step and the next (mod 3)
+    int set, set_next;        // counter sets of this step and the next (mod kSets)
     int ppar;                 // partial buffer of this step; the next step's is ppar ^ 1
     const void* xcur;         // x copy of D read by this step's tiles
     const void* xnext;        // x copy the next step's tiles read (written by this step's solves)
@@ -1264,12 +1268,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
             if (!grid_barrier(p, deadline)) return;
         } else {
             // Operator and solve pass 0, overlapped.  Warps [0, kOpWarps) stream
-            // the operator tiles (HBM-bound); the other warps take 16-row chunks
+            // the operator tiles (HBM-bound); the solver warps take 16-row chunks
             // of every row block whose column chunks are all in and solve them
-            // (FP64-bound), so the two share each SM; the operator warps join
-            // the solving once the tiles are gone.  A row's solve needs only its
-            // own operator products, so the result is the same as running the
-            // phases one after the other.
+            // (FP64-bound), so the two share each SM.  In a step that streams
+            // ahead the operator warps then stream the next step's tiles; in the
+            // last step of a launch they join the solving instead.  A row's
+            // solve needs only its own operator products, so the result is the
+            // same as running the phases one after the other.
             __shared__ int s_fused_fail;
             __shared__ int s_held;       // row chunks this block holds (grabbed, not yet solved)
             __shared__ unsigned long long s_t_solve;
