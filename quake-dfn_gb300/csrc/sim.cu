@@ -671,9 +671,9 @@ __device__ __forceinline__ void reset_counter_set(const SimParams& p, int s, boo
 }
 
 // Claim the next early tile: its index, or -1 once n are claimed, the counter
-// is closed (every block's solves are in), or `stop` blocks have arrived at the
-// step's barrier -- a tile claimed later would still be streaming when the
-// step is decided and hold its block's next step back.  A compare-and-swap, so
+// is closed (every block's solves are in), or p.spec_stop blocks have arrived
+// at the step's barrier (a tile claimed later would still be streaming when
+// the step is decided and hold its block's next step back).  A compare-and-swap, so
 // a closed counter keeps the number of tiles claimed; bounded -- a tile left
 // unclaimed is streamed by its own step.
 __device__ __forceinline__ long long claim_spec(const SimParams& p, unsigned long long* ctr, int64_t n) {
@@ -1411,6 +1411,8 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_sim(SimParams p, int64_t nst
                     }
                 }
                 const uint64_t t_items = gt == 0 ? globaltimer_ns() : 0;
+                // (the last block to arrive closes the next step's early-tile
+                // counter: their number is final for every block leaving it)
                 if (!grid_barrier_solvers(p, deadline, p.spec_ctr + cnext)) {
                     if (gt == 0) s_p3_abort = 1;
                 } else {
