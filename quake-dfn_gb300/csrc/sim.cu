@@ -482,7 +482,9 @@ __device__ __forceinline__ void xload(const X* p, X x[R]) {
 // FP64.  FP32/BF16 storage (kPairs): each partial is the tile's (hi, lo) FP32
 // pair; the hi parts are gathered error-free with TwoSum and the lo parts
 // added, all on the FP32 pipe, and the pair becomes a double once per row.
-// Loads are issued eight chunks at a time so they overlap.
+// Loads are issued in batches (16 chunks per matrix, 8 when one lane sums
+// both; past the last chunk a batch re-reads it and skips the sum), so every
+// batch costs one memory round trip.
 __device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
     return rb >= p.rb_small0 ? p.nchunk2 : p.nchunk;
 }
@@ -498,28 +500,26 @@ __device__ __forceinline__ double sum_partials_side(const SimParams& p, int r, i
     if constexpr (kPairs) {
         const float2* ps = reinterpret_cast<const float2*>(part) + base;
         float h = 0.f, l = 0.f;
-        int c = 0;
-        for (; c + 16 <= nch; c += 16) {
+        for (int c = 0; c < nch; c += 16) {
             float2 t[16];
 #pragma unroll
-            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + (c + k) * cs);
+            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + min(c + k, nch - 1) * cs);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) { two_sum_acc(h, l, t[k].x); l += t[k].y; }
+            for (int k = 0; k < 16; ++k)
+                if (c + k < nch) { two_sum_acc(h, l, t[k].x); l += t[k].y; }
         }
-        for (; c < nch; ++c) { const float2 a = __ldcg(ps + c * cs); two_sum_acc(h, l, a.x); l += a.y; }
         return (double)h + (double)l;
     } else {
         const double* ps = part + base;
         double a = 0;
-        int c = 0;
-        for (; c + 16 <= nch; c += 16) {
+        for (int c = 0; c < nch; c += 16) {
             double t[16];
 #pragma unroll
-            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + (c + k) * cs);
+            for (int k = 0; k < 16; ++k) t[k] = __ldcg(ps + min(c + k, nch - 1) * cs);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) a += t[k];
+            for (int k = 0; k < 16; ++k)
+                if (c + k < nch) a += t[k];
         }
-        for (; c < nch; ++c) a += __ldcg(ps + c * cs);
         return a;
     }
 }
@@ -534,21 +534,20 @@ __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t 
         const float2* ps = reinterpret_cast<const float2*>(p.part_s) + base;
         const float2* pn = reinterpret_cast<const float2*>(p.part_n) + base;
         float hs = 0.f, ls = 0.f, hn = 0.f, ln = 0.f;
-        int c = 0;
-        for (; c + 8 <= nch; c += 8) {
+        for (int c = 0; c < nch; c += 8) {
             float2 ts[8], tn[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
-#pragma unroll
             for (int k = 0; k < 8; ++k) {
-                two_sum_acc(hs, ls, ts[k].x); ls += ts[k].y;
-                two_sum_acc(hn, ln, tn[k].x); ln += tn[k].y;
+                const int cc = min(c + k, nch - 1);   // (past the end: a repeat, not summed)
+                ts[k] = __ldcg(ps + cc * cs);
+                tn[k] = __ldcg(pn + cc * cs);
             }
-        }
-        for (; c < nch; ++c) {
-            const float2 a = __ldcg(ps + c * cs), b = __ldcg(pn + c * cs);
-            two_sum_acc(hs, ls, a.x); ls += a.y;
-            two_sum_acc(hn, ln, b.x); ln += b.y;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (c + k < nch) {
+                    two_sum_acc(hs, ls, ts[k].x); ls += ts[k].y;
+                    two_sum_acc(hn, ln, tn[k].x); ln += tn[k].y;
+                }
         }
         ss = (double)hs + (double)ls;
         sn = (double)hn + (double)ln;
@@ -556,15 +555,18 @@ __device__ __forceinline__ void sum_partials(const SimParams& p, int r, int64_t 
         const double* ps = p.part_s + base;
         const double* pn = p.part_n + base;
         double as = 0, an = 0;
-        int c = 0;
-        for (; c + 8 <= nch; c += 8) {
+        for (int c = 0; c < nch; c += 8) {
             double ts[8], tn[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) { ts[k] = __ldcg(ps + (c + k) * cs); tn[k] = __ldcg(pn + (c + k) * cs); }
+            for (int k = 0; k < 8; ++k) {
+                const int cc = min(c + k, nch - 1);   // (past the end: a repeat, not summed)
+                ts[k] = __ldcg(ps + cc * cs);
+                tn[k] = __ldcg(pn + cc * cs);
+            }
 #pragma unroll
-            for (int k = 0; k < 8; ++k) { as += ts[k]; an += tn[k]; }
+            for (int k = 0; k < 8; ++k)
+                if (c + k < nch) { as += ts[k]; an += tn[k]; }
         }
-        for (; c < nch; ++c) { as += __ldcg(ps + c * cs); an += __ldcg(pn + c * cs); }
         ss = as;
         sn = an;
     }
