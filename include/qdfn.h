@@ -258,6 +258,40 @@ int qdfn_get_kself(const qdfn_ctx* ctx, double* kself);
 int qdfn_apply_dense_noalloc(int64_t N, const double* Ks, const double* Kn, int64_t ld,
                              const double* D, double* tld, double* knd, void* stream);
 
+/* ---- input parsing and discretisation (host only) ------------------------ */
+/* The reference's RUN2 front end, so a caller goes from the bulk text file to
+ * the segment table without Julia.  Tables are row-major doubles.  Two-call
+ * pattern: with seg == NULL only the sizes are returned. */
+typedef struct qdfn_bulk_info {
+    double switch_ss_rn;             /* 1 strike-slip, 2 reverse/normal (LRtoRake) */
+    double shear_modulus, poisson_ratio, rock_density;
+    double drop_crit, drop_crit_ns_multiplier, minimum_ns;
+    int32_t is_triangle;             /* 0: rectangles, 1: triangles */
+    int32_t columns;                 /* segment columns: 19 (rectangles) or 20 (triangles) */
+    int64_t fault_count;             /* segment rows */
+    int64_t loading_fault_count;     /* rows with a constant loading velocity (sorted last) */
+} qdfn_bulk_info;
+
+/* Replaces ReadBulkInput (scripts/Functions_BuildInputFile.jl:216-274, with
+ * LRtoRake :182-213 and BulkToSegment :82-179): parses the 18-column
+ * (rectangle) or 20-column (triangle) bulk file, sorts by the loading column,
+ * converts the +-1 slip sense to rake, grids rectangles into patches, and
+ * writes `fault_count` rows of `columns` values to seg (cap_rows rows of room).
+ * Malformed files return QDFN_ERR_INVALID (the reference raises). */
+int qdfn_read_bulk_input(const char* path, qdfn_bulk_info* info, double* seg, int64_t cap_rows);
+
+/* Replaces BulkToSegment (scripts/Functions_BuildInputFile.jl:82-179): nbulk
+ * rows of 18 values (rake in degrees) to *nseg rows of 19. */
+int qdfn_bulk_to_segment(int64_t nbulk, const double* bulk, double* seg, int64_t cap_rows, int64_t* nseg);
+
+/* Replaces RotVerts_UnitVectors (scripts/Functions_BuildInputFile.jl:338-377):
+ * per triangle (n x 3 vertex arrays) swaps P1/P2 where the unit normal's y
+ * component is <= 0, then writes the unit normal, strike, dip and slip
+ * vectors (rake in degrees). */
+int qdfn_rot_verts_unit_vectors(int64_t n, const double* P1in, const double* P2in, const double* P3in,
+                                const double* rake, double* P1, double* P2, double* P3, double* un,
+                                double* us, double* ud, double* uslip);
+
 #ifdef __cplusplus
 }
 #endif

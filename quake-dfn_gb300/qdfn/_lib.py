@@ -31,8 +31,16 @@ EXPORTS = [
     "qdfn_get_counters",
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
     "qdfn_apply_dense_noalloc", "qdfn_set_state_all", "qdfn_get_state_all", "qdfn_set_blocks",
-    "qdfn_get_blocks",
+    "qdfn_get_blocks", "qdfn_read_bulk_input", "qdfn_bulk_to_segment", "qdfn_rot_verts_unit_vectors",
 ]
+
+
+class BulkInfo(C.Structure):
+    """Mirror of struct qdfn_bulk_info."""
+    _fields_ = [(n, C.c_double) for n in ("switch_ss_rn", "shear_modulus", "poisson_ratio", "rock_density",
+                                          "drop_crit", "drop_crit_ns_multiplier", "minimum_ns")] + \
+               [("is_triangle", C.c_int32), ("columns", C.c_int32), ("fault_count", C.c_int64),
+                ("loading_fault_count", C.c_int64)]
 
 
 class QdfnError(RuntimeError):
@@ -103,6 +111,9 @@ def load():
     L.qdfn_get_kself.argtypes = [C.c_void_p, _dp]
     L.qdfn_apply_dense_noalloc.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
+    L.qdfn_read_bulk_input.argtypes = [C.c_char_p, C.POINTER(BulkInfo), C.c_void_p, C.c_int64]
+    L.qdfn_bulk_to_segment.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    L.qdfn_rot_verts_unit_vectors.argtypes = [C.c_int64] + [C.c_void_p] * 11
     _lib = L
     return L
 

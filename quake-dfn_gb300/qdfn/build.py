@@ -23,6 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # translation unit -> extra flags
 UNITS = {
     "api.cpp": [],
+    "input.cpp": [],
     "assemble.cu": [],
     "assemble_rect.cu": ["--fmad=false"],
     "assemble_tri.cu": ["--fmad=false"],

@@ -248,3 +248,51 @@ def rect_records(d):
     return np.ascontiguousarray(np.column_stack([c[:, 0], c[:, 1], c[:, 2], d["FaultLengthStrike"],
                                                  d["FaultLengthDip"], d["FaultStrikeAngle"],
                                                  d["FaultDipAngle"], d["FaultRakeAngle"]]), dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# The same front end through the C ABI (qdfn_read_bulk_input,
+# qdfn_bulk_to_segment, qdfn_rot_verts_unit_vectors): the entry points a
+# non-Python caller (the Julia shim) uses.
+def _abi():
+    from . import _lib
+    return _lib, _lib.load()
+
+
+def read_bulk_input_abi(path):
+    """read_bulk_input through the C ABI; same keys."""
+    import ctypes as C
+    _lib, L = _abi()
+    info = _lib.BulkInfo()
+    _lib.check(L.qdfn_read_bulk_input(path.encode(), C.byref(info), None, 0))
+    seg = np.zeros((info.fault_count, info.columns))
+    _lib.check(L.qdfn_read_bulk_input(path.encode(), C.byref(info), seg.ctypes.data, seg.shape[0]))
+    return dict(Switch_StrikeSlip_or_ReverseNormal=info.switch_ss_rn, ShearModulus=info.shear_modulus,
+                PoissonRatio=info.poisson_ratio, RockDensity=info.rock_density, DropCrit=info.drop_crit,
+                DropCritNormalStressMultiplier=info.drop_crit_ns_multiplier, MinimumNS=info.minimum_ns,
+                RorT="T" if info.is_triangle else "R", Input_Segment=seg,
+                LoadingFaultCount=int(info.loading_fault_count), FaultCount=int(info.fault_count))
+
+
+def bulk_to_segment_abi(bulk):
+    """bulk_to_segment through the C ABI."""
+    import ctypes as C
+    _lib, L = _abi()
+    bulk = np.ascontiguousarray(bulk, dtype=np.float64)
+    n = C.c_int64(0)
+    _lib.check(L.qdfn_bulk_to_segment(bulk.shape[0], bulk.ctypes.data, None, 0, C.byref(n)))
+    seg = np.zeros((n.value, 19))
+    _lib.check(L.qdfn_bulk_to_segment(bulk.shape[0], bulk.ctypes.data, seg.ctypes.data, seg.shape[0], C.byref(n)))
+    return seg
+
+
+def rot_verts_unit_vectors_abi(seg, rake):
+    """rot_verts_unit_vectors through the C ABI."""
+    _lib, L = _abi()
+    n = seg.shape[0]
+    P = [np.ascontiguousarray(seg[:, 3 * k:3 * k + 3], dtype=np.float64) for k in range(3)]
+    rk = np.ascontiguousarray(rake, dtype=np.float64)
+    out = [np.zeros((n, 3)) for _ in range(7)]
+    _lib.check(L.qdfn_rot_verts_unit_vectors(n, *(a.ctypes.data for a in P), rk.ctypes.data,
+                                              *(a.ctypes.data for a in out)))
+    return tuple(out)
