@@ -89,12 +89,15 @@ def green_functions(points, centres, lengths, compressibility, G, pi=REFERENCE_P
 
 
 def fault_forcing(centre, strike, dip, rake, G, nu, cuboid_centres, cuboid_lengths, times, pore_pressure,
-                  temperature=None, thermal_expansivity=1e-5, biot=1.0, pi=REFERENCE_PI):
+                  temperature=None, thermal_expansivity=1e-5, biot=1.0, pi=REFERENCE_PI, normals=None, slips=None):
     """External-stress forcing on the fault patches (centre n x 3, depth
     positive; angles in degrees) from the cuboids' pore-pressure and
     temperature changes (nt x n_cuboids).  Returns dict(t, normal, shear,
-    pressure) with nt x n arrays, plus the rotated-frame inputs (poro_stress
-    6 x nt x n, compression positive; poro_disp 3 x nt x n)."""
+    pressure) with nt x n arrays, plus the inputs of the projection
+    (poro_stress 6 x nt x n, compression positive; poro_disp 3 x nt x n).
+    Triangles (CalculatePoroElasticStress_Tri.jl:182-256): pass the unit
+    normals and slip vectors (n x 3) instead; the traction on the normal is
+    projected on them and strike/dip/rake are not used."""
     centre = np.asarray(centre, dtype=float)
     pw = 2 * G * (1 - nu) / (1 - 2 * nu)               # P-wave modulus
     cm = 1 / pw
@@ -114,6 +117,12 @@ def fault_forcing(centre, strike, dip, rake, G, nu, cuboid_centres, cuboid_lengt
     eff = np.stack([np.stack([s11 + p_fault, s12, s13], -1),
                     np.stack([s12, s22 + p_fault, s23], -1),
                     np.stack([s13, s23, s33 + p_fault], -1)], -2)                  # nt x n x 3 x 3
+    if normals is not None:
+        nv = np.asarray(normals, dtype=float)
+        tr = np.einsum("tnij,nj->tni", eff, nv)                                   # traction on the patch
+        return dict(t=np.asarray(times, dtype=float), normal=-np.einsum("tni,ni->tn", tr, nv),
+                    shear=np.einsum("tni,ni->tn", tr, np.asarray(slips, dtype=float)), pressure=p_fault,
+                    poro_stress=stress, poro_disp=disp)
     strike, dip, rake = (np.asarray(a, dtype=float) for a in (strike, dip, rake))
     Rs = np.zeros((centre.shape[0], 3, 3))
     Rd = np.zeros_like(Rs)

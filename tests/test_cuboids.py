@@ -109,3 +109,28 @@ def test_input_files_and_forcing(tmp_path):
     assert out["normal"][2, 2] == pytest.approx(-sf[2, 2], rel=1e-12, abs=1e-6)
     assert out["shear"][2, 2] == pytest.approx(Gm.cosd(180.0) * sf[0, 2] + Gm.sind(180.0) * sf[1, 2], rel=1e-12,
                                                abs=1e-6)
+
+
+def test_triangle_projection_agrees_with_the_rotation():
+    """For a patch given by its unit normal and slip vector the traction
+    projection equals the strike/dip rotation of the rectangle path."""
+    rng = np.random.default_rng(5)
+    n = 6
+    fc = np.column_stack([rng.uniform(-2e3, 2e3, n), rng.uniform(-2e3, 2e3, n), rng.uniform(2e3, 4e3, n)])
+    strike, dip, rake = rng.uniform(0, 180, n), rng.uniform(30, 90, n), rng.uniform(-180, 180, n)
+    cen, lens = np.array([[0.0, 0.0, 3000.0]]), np.array([[3000.0, 3000.0, 300.0]])
+    t = np.array([0.0, 1e8])
+    pp = np.array([[0.0], [-1e7]])
+    a = Cb.fault_forcing(fc, strike, dip, rake, 3e10, 0.25, cen, lens, t, pp)
+    nv, sv = np.zeros((n, 3)), np.zeros((n, 3))
+    for i in range(n):
+        Rs = np.array([[Gm.cosd(-strike[i]), -Gm.sind(-strike[i]), 0], [Gm.sind(-strike[i]), Gm.cosd(-strike[i]), 0],
+                       [0, 0, 1]])
+        Rd = np.array([[1, 0, 0], [0, Gm.cosd(-dip[i]), -Gm.sind(-dip[i])], [0, Gm.sind(-dip[i]), Gm.cosd(-dip[i])]])
+        Rm = Rd @ Rs
+        nv[i] = Rm[2]
+        sv[i] = Gm.cosd(rake[i]) * Rm[0] + Gm.sind(rake[i]) * Rm[1]
+    b = Cb.fault_forcing(fc, None, None, None, 3e10, 0.25, cen, lens, t, pp, normals=nv, slips=sv)
+    assert np.allclose(a["normal"], b["normal"], rtol=1e-10, atol=1e-4)
+    assert np.allclose(a["shear"], b["shear"], rtol=1e-10, atol=1e-4)
+    assert np.array_equal(a["pressure"], b["pressure"])
