@@ -73,6 +73,26 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, dev):
+    """The largest x over the ranks of the default process group (every rank
+    gets it): the job's time is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, dev):
+    """The sum of x over the ranks (every rank gets it): the job's work is all
+    ranks' work."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t)
+    return float(t.item())
+
+
 def workload(args):
     from qdfn import synth
     sysd = synth.fault_network(seed=args.seed, n_faults=args.faults)
@@ -236,17 +256,13 @@ def run_ours(args):
     cnt1 = sim.counters()
     phases = {k: cnt1[k] - cnt0[k] for k in cnt1}
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         torch.distributed.barrier()
     T1 = total_sim_time(sim, R)
     sim_years = float(np.sum(T1 - T0)) / YEAR
     end_state0 = sim.state(0)
     if ws > 1:
-        t = torch.tensor([sim_years], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t)
-        sim_years_all = float(t.item())
+        sim_years_all = sum_over_ranks(sim_years, dev)
     else:
         sim_years_all = sim_years
     value = sim_years_all / (ms / 1e3 / 3600.0)
