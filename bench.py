@@ -59,10 +59,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="network", choices=["network", "ensemble"],
-                    help="network: the 30-fault network (default); ensemble: 64 geometries of "
-                         "800-6,000 patches x 4 friction draws advanced together")
+    ap.add_argument("--workload", default="ensemble", choices=["network", "ensemble"],
+                    help="ensemble (default, C4): 64 fault networks of 800-6,000 patches x 4 friction draws in "
+                         "one persistent launch; network (C2): the 30-fault network x 4 draws")
     ap.add_argument("--geometries", type=int, default=64)
+    ap.add_argument("--cpu-members", type=int, default=4,
+                    help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
+    ap.add_argument("--horizon", type=int, default=1000,
+                    help="steps of the mixed-vs-FP64 accuracy horizon (from t = 0)")
     return ap.parse_args()
 
 
@@ -526,60 +530,407 @@ def ensemble_geometries(n_geo, seed=11):
     return out
 
 
-def run_ensemble(args):
-    """Batched ensemble: every geometry with its friction draws is one
-    context on a share of the SMs, all advanced together (qdfn.ensemble)."""
+def _member_sample(sizes, k):
+    """k member indices at evenly spaced size quantiles (smallest to largest),
+    so that a bounded CPU sample spans the ensemble's size range."""
+    order = np.argsort(sizes, kind="stable")
+    pick = sorted(set(int(order[int(round(q * (len(order) - 1)))]) for q in np.linspace(0.0, 1.0, k)))
+    return pick
+
+
+def _snapshot(ens):
+    return [[sim.state(r) for r in range(sim.n_inst)] for sim in ens.members]
+
+
+def _restore(ens, snap):
+    for sim, sts in zip(ens.members, snap):
+        for r, st in enumerate(sts):
+            sim.set_state(r, st)
+
+
+def _ens_slip_err(a, b):
+    """Per-instance relative slip error max|D_a - D_b| / max|D_b|, a vs b."""
+    out = []
+    for sa, sb in zip(a.members, b.members):
+        for r in range(sa.n_inst):
+            da, db = sa.state(r)["D"], sb.state(r)["D"]
+            out.append(float(np.max(np.abs(da - db)) / max(np.max(np.abs(db)), 1e-300)))
+    return np.asarray(out)
+
+
+def fp64_peak_tflops(dev):
+    """FP64 matrix-multiply throughput of this GPU through the vendor library
+    (torch.matmul on float64, 4096^3, best of 3) -- the measured FP64 peak the
+    FP64-bound kernels are compared with."""
     import torch
-    from qdfn import assemble, ensemble, synth
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(0)
-    geos = ensemble_geometries(args.geometries)
-    members = []
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
+
+
+def profiled(name):
+    """A committed ncu summary (profiles/<name>.json) or None."""
+    p = os.path.join(ROOT, "profiles", name + ".json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+def build_ensemble(args, dev, rank=0):
+    """The C4 ensemble: geometries with 3-40 faults and 800-6,000 patches,
+    each with `inst` friction draws; FP64 stiffness assembled on the GPU.
+    Returns the member dicts (device FP64 K), per-geometry host data and the
+    assembly time."""
+    import torch
+    from qdfn import assemble, synth
+    geos = ensemble_geometries(args.geometries, seed=11 + 1000 * rank)
+    members, info = [], []
+    asm_ms, pairs = 0.0, 0
     for g, sysd in enumerate(geos):
         N = sysd["N"]
         rec = torch.tensor(sysd["records"], dtype=torch.float64, device=dev)
         Ks = torch.empty((N, N), dtype=torch.float64, device=dev)
         Kn = torch.empty((N, N), dtype=torch.float64, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         assemble.assemble_rect_dev(rec, rec, sysd["G"], sysd["nu"], Ks, Kn, layout="col")
+        e1.record()
+        torch.cuda.synchronize()
+        asm_ms += e0.elapsed_time(e1)
+        pairs += N * N
         kdiag = torch.diagonal(Ks).cpu().numpy()
         draws = synth.friction_draws(sysd, args.inst, seed=g + 1)
         prob = synth.problem_dict(sysd, kdiag, n_inst=args.inst, draws=draws)
         ext = synth.external_ramp(N, sysd["stressing_rate"], 1e12)
         members.append(dict(problem=prob, n_inst=args.inst, Ks=Ks, Kn=Kn, ext=ext))
+        info.append(dict(sysd=sysd, draws=draws, kdiag=kdiag, ext=ext, N=N))
+    return members, info, asm_ms, pairs
+
+
+def _oracle_member(oracle, info_g, inst, Ks, Kn, nthreads):
+    N = info_g["N"]
+    p = problem(info_g["sysd"], {k: v[inst * N:(inst + 1) * N] for k, v in info_g["draws"].items()},
+                info_g["kdiag"], 1)
+    ext = info_g["ext"]
+    p.update(ext_t=ext["t"], ext_n=ext["normal"], ext_s=ext["shear"], ext_p=ext["pressure"])
+    return oracle.Simulation(p, ("dense", Ks, Kn), nthreads=nthreads)
+
+
+def ensemble_cpu_sample(args, info, hostK, start, budget_s):
+    """FP64 CPU oracle (all host threads) on instance 0 of the sampled members,
+    each from its state at the timed window's start, for a share of
+    `budget_s`; sim-years/hour = their summed simulated time over their summed
+    wall time."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    nth = os.cpu_count()
+    yrs, wall, done = 0.0, 0.0, []
+    for g, (Ks, Kn) in hostK.items():
+        s = _oracle_member(oracle, info[g], 0, Ks, Kn, nth)
+        st = start[g][0]
+        for k in ("V", "D", "theta", "friction", "accel", "sigma_old"):
+            s.state[k][:] = st[k]
+        s.set_scalars(st["T"], st["dt"], st["step"])
+        t0 = time.perf_counter()
+        s.run(1)
+        one = time.perf_counter() - t0
+        k = int(max(1, min(args.steps - 1, (budget_s / len(hostK)) / max(one, 1e-6))))
+        s.run(k)
+        w = time.perf_counter() - t0
+        yrs += (s.T - st["T"]) / YEAR
+        wall += w
+        done.append((g, info[g]["N"], k + 1))
+    return {"value": yrs / (wall / 3600.0), "unit": "sim-years/hour", "cores": nth, "kind": "port",
+            "sample": "instance 0 of members %s (%s patches) for %s steps from the timed window's start, FP64 "
+                      "CPU oracle (C++ restatement of the reference algorithm), all host threads"
+                      % ([d[0] for d in done], [d[1] for d in done], [d[2] for d in done]),
+            "wall_s": wall}
+
+
+def run_ensemble(args):
+    """C4, the headline: 64 fault networks of uneven size x 4 friction draws
+    (256 instances) advanced by ONE persistent launch (qdfn_ensemble_*),
+    operator in FP32 with FP64 state; beside it the same ensemble with the
+    FP64 operator (the plain FP64 GPU path), the accuracy horizon of the mixed
+    run against it, the end-to-end rate through the C ABI with host buffers,
+    and the FP64 CPU oracle on a sample of the same members."""
+    import torch
+    from qdfn import ensemble
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    members, info, asm_ms, pairs = build_ensemble(args, dev, rank)
+    sizes = [g["N"] for g in info]
+    R = args.inst
+    sample = _member_sample(sizes, args.cpu_members)
+    hostK = {}
+    if rank == 0 and not args.no_cpu:
+        for g in sample:   # (src, recv) buffers: K[recv, src] is their transpose
+            hostK[g] = (members[g]["Ks"].cpu().numpy().T, members[g]["Kn"].cpu().numpy().T)
     ens = ensemble.Ensemble(members, precision=args.precision)
+    ens64 = None if args.no_fp64 else ensemble.Ensemble(members, precision="fp64")
     del members
     torch.cuda.empty_cache()
-    ens.run(args.warmup, timeout_s=TIMEOUT)
+    s0 = _snapshot(ens)
+
+    # ---- accuracy horizon: mixed vs FP64 from t = 0, every 100 steps
+    horizon = None
+    if ens64 is not None:
+        total = min(args.warmup + args.steps, args.horizon)
+        errs, done = [], 0
+        while done < total:
+            n = min(100, total - done)
+            ens.run(n, timeout_s=TIMEOUT)
+            ens64.run(n, timeout_s=TIMEOUT)
+            done += n
+            e = _ens_slip_err(ens, ens64)
+            errs.append((done, float(e.max()), float(np.median(e)), int(np.sum(e <= 1e-6))))
+        first_bad = next((st for st, mx, _, _ in errs if mx > 1e-6), None)
+        horizon = {"checked_every": 100, "instances": int(len(sizes) * R),
+                   "steps_all_within_1e-6": (first_bad - 100) if first_bad else total,
+                   "first_step_above_1e-6": first_bad,
+                   "at_step": {str(st): {"max": mx, "median": md, "instances_within_1e-6": k}
+                               for st, mx, md, k in errs}}
+        _restore(ens, s0)
+        _restore(ens64, s0)
+
+    # ---- warm-up with the autotuner (SM shares re-divided by measured member time)
+    shares0 = [int(b) for b in ens.blocks]
+    ens.autotune(args.warmup, rounds=3, timeout_s=TIMEOUT)
     y0 = ens.sim_years()
+    start = _snapshot(ens)
+
+    # ---- timed: one persistent launch over K steps of every member
+    clocks = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(0)
     clocks.start()
     time.sleep(0.3)
-    t0 = time.perf_counter()
-    ens.run(args.steps, timeout_s=TIMEOUT)
+    cnt0 = [sim.counters() for sim in ens.members]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ens.run_async(args.steps, timeout_s=TIMEOUT, stream=stream.cuda_stream)
+    ev1.record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    ens.sync()
     clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        ms = max_over_ranks(ms, dev)
+        torch.distributed.barrier()
     yrs = float(np.sum(ens.sim_years() - y0))
-    sizes = [m.N for m in ens.members]
-    line = {"metric": "ensemble sim-years/hour (batched geometries)", "value": yrs / (wall / 3600.0),
-            "unit": "sim-years/hour", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "%s-operator/fp64-state" % args.precision, "data": "synthetic",
-            "config": {"workload": "%d geometries of %d-%d patches (%d total) x %d friction draws, one context "
-                                   "per geometry on its share of the SMs, all advanced together"
-                                   % (len(sizes), min(sizes), max(sizes), sum(sizes), args.inst),
-                       "instances": len(sizes) * args.inst, "precision": args.precision,
-                       "sm_shares": [int(b) for b in ens.blocks]},
-            "gpu_launches": len(sizes), "clocks": clk,
-            "note": "wall clock over all members' concurrent launches (each member takes its own adaptive steps)"}
+    yrs_all = sum_over_ranks(yrs, dev) if ws > 1 else yrs
+    value = yrs_all / (ms / 1e3 / 3600.0)
+    steps_done = [sim.state(r)["step"] - start[m][r]["step"] for m, sim in enumerate(ens.members)
+                  for r in range(sim.n_inst)]
+
+    # ---- roofline of the persistent kernel (the one long launch of the window)
+    esz = {"fp32": 4, "bf16x2": 4, "fp64": 8}[args.precision]
+    mat_bytes = sum(2 * n * n * esz for n in sizes)
+    vec_bytes = sum(R * n * 8 * 14 for n in sizes)
+    alg_bytes = args.steps * (mat_bytes + vec_bytes)
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    prof = profiled("k_sim_members_c4_fp32")
+    traffic = None
+    if prof and prof.get("instances") == len(sizes) * R and prof.get("total_patches") == sum(sizes):
+        traffic = float(prof["dram_bytes_per_step"]) * args.steps
+    cnt = [sim.counters() for sim in ens.members]
+    solves = sum(c1["lowv_solves"] + c1["highv_solves"] - c0["lowv_solves"] - c0["highv_solves"]
+                 for c0, c1 in zip(cnt0, cnt))
+    fp64_tf = fp64_peak_tflops(dev) if rank == 0 else None
+
+    # ---- FP64 GPU path on the same ensemble and window
+    fp64 = None
+    if ens64 is not None:
+        ens64.autotune(args.warmup, rounds=3, timeout_s=TIMEOUT)
+        z0 = ens64.sim_years()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        ens64.run_async(args.steps, timeout_s=TIMEOUT, stream=stream.cuda_stream)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ens64.sync()
+        ms64 = f0.elapsed_time(f1)
+        yrs64 = float(np.sum(ens64.sim_years() - z0))
+        # the FP64 operator products are FP64-FMA bound: 2 matrices x R draws
+        # x 2 flops per stored entry and step
+        fl64 = args.steps * sum(2 * n * n * R * 2 for n in sizes)
+        fp64 = {"value": yrs64 / (ms64 / 1e3 / 3600.0), "unit": "sim-years/hour", "ms_per_step": ms64 / args.steps,
+                "instances": int(len(sizes) * R),
+                "mixed_over_fp64": (yrs / (ms / 3.6e6)) / (yrs64 / (ms64 / 3.6e6)),
+                "roofline": {"bound": "fp64", "achieved": fl64 / (ms64 / 1e3) / 1e12, "unit": "TFLOP/s",
+                             "peak": fp64_tf, "frac": (fl64 / (ms64 / 1e3) / 1e12) / fp64_tf if fp64_tf else None,
+                             "note": "operator FP64 FMAs (2 matrices x R x 2 flop per entry and step) over the "
+                                     "launch; peak = torch.matmul float64 4096^3 measured in this run"}}
+        ens64.close()
+        ens64 = None
+        torch.cuda.empty_cache()
+
+    # ---- e2e through the C ABI with host buffers: every step, every member's
+    # state goes up from pinned host memory, one ensemble step runs (one
+    # launch), the state comes back; one synchronisation per step
+    e2e = None
+    if not args.no_e2e:
+        _restore(ens, start)
+        names = ensemble.simulate.Simulation.STATE_FIELDS
+        bufs = []
+        for m, sim in enumerate(ens.members):
+            blk = torch.empty((len(names), sim.n_inst, sim.N), dtype=torch.float64).pin_memory()
+            for f, k in enumerate(names):
+                blk[f].copy_(torch.from_numpy(np.stack([start[m][r][k] for r in range(sim.n_inst)])))
+            Tdt = torch.tensor([[start[m][r]["T"] for r in range(sim.n_inst)],
+                                [start[m][r]["dt"] for r in range(sim.n_inst)]], dtype=torch.float64).pin_memory()
+            stp = torch.tensor([start[m][r]["step"] for r in range(sim.n_inst)], dtype=torch.int64).pin_memory()
+            bufs.append(({k: blk[f] for f, k in enumerate(names)}, Tdt, stp))
+        sptr = stream.cuda_stream
+        nbytes = sum(6 * sim.n_inst * sim.N * 8 + sim.n_inst * 24 for sim in ens.members)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for sim, (arr, Tdt, stp) in zip(ens.members, bufs):
+                sim.set_state_all(arr, Tdt[0], Tdt[1], stp, stream=sptr)
+            ens.run_async(1, timeout_s=TIMEOUT, stream=sptr)
+            for sim, (arr, Tdt, stp) in zip(ens.members, bufs):
+                sim.get_state_all(arr, Tdt[0], Tdt[1], stp, stream=sptr, wait=False)
+            ens.sync()
+        t_e2e = time.perf_counter() - t0
+        if ws > 1:
+            t_e2e = max_over_ranks(t_e2e, dev)
+        ye = sum(float(bufs[m][1][0][r].item() - start[m][r]["T"]) for m, sim in enumerate(ens.members)
+                 for r in range(sim.n_inst)) / YEAR
+        if ws > 1:
+            ye = sum_over_ranks(ye, dev)
+        e2e = {"value": ye / (t_e2e / 3600.0), "unit": "sim-years/hour", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes,
+               "note": "one ensemble step per launch (no step streams ahead across a launch boundary)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = ensemble_cpu_sample(args, info, hostK, start, args.cpu_sample_s)
+
+    if rank == 0:
+        tot = sum(sizes)
+        line = {
+            "metric": "ensemble sim-years/hour, mixed-prec vs FP64 on GPU at <=1e-6 rel slip error",
+            "value": value, "unit": "sim-years/hour", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32-operator/fp64-state" if args.precision != "fp64" else "fp64",
+            "data": "synthetic (seeded fault networks with the reference's fault-network distributions; the "
+                    "reference ships no benchmark data)",
+            "config": {"workload": "C4 batched ensemble: %d fault networks of %d-%d patches (%d total, 3-40 faults "
+                                   "each) x %d friction draws = %d instances, one persistent launch, operator %s"
+                                   % (len(sizes), min(sizes), max(sizes), tot, R, len(sizes) * R, args.precision),
+                       "instances": len(sizes) * R, "geometries": len(sizes), "total_patches": tot,
+                       "precision": args.precision, "parallelism": "replicas",
+                       "l2": "operator %.2f GB per ensemble step > 129 MB L2 (no flush needed)" % (mat_bytes / 1e9),
+                       "sm_shares_initial": shares0, "sm_shares_tuned": [int(b) for b in ens.blocks],
+                       "steps_per_instance": [int(min(steps_done)), int(max(steps_done))],
+                       "sim_years_in_window": yrs_all},
+            "gpu_launches": 3,
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "note": "k_sim_members (one launch, every member's K steps), algorithmic bytes = K x "
+                                 "sum over members (2 N^2 x %d B operator + state vectors); peak %s. The small "
+                                 "members are bound by their FP64 friction solves, not by HBM: %.3g patch solves "
+                                 "per second" % (esz, peak_kind, solves / max(ms / 1e3, 1e-9))},
+            "cpu_baseline": cpu,
+            "fp64_gpu": fp64,
+            "accuracy_horizon": horizon,
+            "assembly": {"pairs": pairs, "ms": asm_ms, "pairs_per_s": pairs / (asm_ms / 1e3),
+                         "fp64_peak_tflops_measured": fp64_tf},
+            "clocks": clk,
+        }
+        asm_prof = profiled("k_assemble_rect_fp64")
+        if asm_prof and fp64_tf:
+            fl = float(asm_prof["fp64_flop_per_pair"]) * pairs / (asm_ms / 1e3) / 1e12
+            line["assembly"].update(fp64_flop_per_pair=asm_prof["fp64_flop_per_pair"], fp64_tflops=fl,
+                                    fp64_frac=fl / fp64_tf)
+        print(json.dumps(line))
+    ens.close()
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def run_reference_ensemble(args):
+    """Reference arm for C4: the FP64 CPU oracle (the reference's algorithm
+    restated in C++; the Julia reference itself cannot run here) on instance 0
+    of sampled members of the same ensemble (same seeds and draws), over the
+    whole window, all host threads."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from qdfn import synth
+    geos = ensemble_geometries(args.geometries)
+    sizes = [g["N"] for g in geos]
+    nth = os.cpu_count()
+    yrs, wall, done = 0.0, 0.0, []
+    for g in _member_sample(sizes, args.cpu_members):
+        sysd = geos[g]
+        rec = sysd["records"]
+        cols = dict(cx=rec[:, 0], cy=rec[:, 1], cz=rec[:, 2], ls=rec[:, 3], ld=rec[:, 4], strike=rec[:, 5],
+                    dip=rec[:, 6], rake=rec[:, 7])
+        Ks, Kn = oracle.assemble_rect(cols, cols, sysd["G"], sysd["nu"], nthreads=nth)
+        kdiag = np.diag(Ks).copy()
+        draws = synth.friction_draws(sysd, args.inst, seed=g + 1)
+        ext = synth.external_ramp(sysd["N"], sysd["stressing_rate"], 1e12)
+        s = _oracle_member(oracle, dict(sysd=sysd, draws=draws, kdiag=kdiag, ext=ext, N=sysd["N"]), 0, Ks, Kn, nth)
+        del Ks, Kn
+        s.run(args.warmup)
+        T0 = s.T
+        t0 = time.perf_counter()
+        s.run(args.steps)
+        wall += time.perf_counter() - t0
+        yrs += (s.T - T0) / YEAR
+        done.append((g, sysd["N"]))
+    value = yrs / (wall / 3600.0)
+    sample = ("instance 0 of members %s (%s patches) of the C4 ensemble (same seeds and draws), the whole window "
+              "(%d warm-up + %d timed steps), FP64 C++ restatement of the reference algorithm (Julia is not "
+              "available), all host threads" % ([d[0] for d in done], [d[1] for d in done], args.warmup, args.steps))
+    line = {"impl": "reference",
+            "metric": "ensemble sim-years/hour, mixed-prec vs FP64 on GPU at <=1e-6 rel slip error",
+            "value": value, "unit": "sim-years/hour", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall / args.steps / len(done) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded fault networks)",
+            "config": {"workload": "C4 batched ensemble: %d fault networks of %d-%d patches x %d friction draws "
+                                   "(sampled members, see cpu_baseline.sample)"
+                                   % (len(sizes), min(sizes), max(sizes), args.inst),
+                       "instances": len(sizes) * args.inst, "parallelism": "cpu-threads"},
+            "cpu_baseline": {"value": value, "unit": "sim-years/hour", "cores": nth, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "sim-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 def main():
     args = parse()
     if args.impl == "reference":
-        run_reference(args)
+        run_reference_ensemble(args) if args.workload == "ensemble" else run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
     else:

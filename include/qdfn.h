@@ -187,6 +187,50 @@ int qdfn_kernels_per_run(const qdfn_ctx* ctx);
  * reference, which runs one geometry per process. */
 int qdfn_set_blocks(qdfn_ctx* ctx, int nblocks);
 int qdfn_get_blocks(const qdfn_ctx* ctx);
+
+/* ---- ensembles: many contexts in one persistent launch ------------------- */
+/* Batched ensembles of fault networks of uneven size (no counterpart in the
+ * reference, which runs one geometry per Julia process; each member is the
+ * state of one `main` call, scripts/Functions_RSFDFN3DMain_D.jl:2-324).  An
+ * ensemble advances n member contexts -- each with its own dense operator, up
+ * to 4 friction draws, state, external stress and adaptive time steps -- in ONE
+ * cooperative launch: member k runs on its own contiguous range of blocks (its
+ * share of the SMs) with its own grid barrier, so members never wait on one
+ * another, and one grid holds them all, so every member's blocks are
+ * co-resident by the cooperative launch's guarantee.  All members must hold a
+ * dense operator of the same precision and the same instance count class
+ * (1, 2 or 3-4).  Members stay ordinary contexts (their state, history and
+ * counter calls work between runs); while an ensemble run is in flight, run
+ * no member on its own.  Destroy the ensemble before its members (a member
+ * destroyed first makes later ensemble runs fail with QDFN_ERR_STATE).
+ *
+ * blocks: blocks per member (each >= 1), or NULL for a split proportional to
+ * an estimate of each member's per-step cost (operator bytes + patch solves).
+ * The sum must fit on the GPU at once (one block per SM), so n <= SM count. */
+typedef struct qdfn_ensemble qdfn_ensemble;
+int qdfn_ensemble_create(qdfn_ensemble** out, int n, qdfn_ctx* const* members, const int* blocks);
+int qdfn_ensemble_destroy(qdfn_ensemble* ens);
+/* Blocks each member runs on (n ints). */
+int qdfn_ensemble_get_blocks(const qdfn_ensemble* ens, int* blocks);
+/* Re-divides the SMs (NULL: the cost estimate). */
+int qdfn_ensemble_set_blocks(qdfn_ensemble* ens, const int* blocks);
+/* Autotuner step: re-divides the SMs in proportion to each member's measured
+ * cost since the last balance (its busy time on the device times its blocks),
+ * so that members taking the same number of steps finish together.  Call it
+ * between runs, e.g. a few times during warm-up.  The column chunking of a
+ * member's FP32/BF16 products follows its block count, so a new split can
+ * change results in the last bits of the operator sums. */
+int qdfn_ensemble_balance(qdfn_ensemble* ens);
+/* Advances every instance of every member by nsteps of its own time steps in
+ * one launch (timeout_s as for qdfn_run, per member).  _async enqueues on
+ * `stream`; qdfn_ensemble_sync waits and returns the first failing member's
+ * status. */
+int qdfn_ensemble_run(qdfn_ensemble* ens, int64_t nsteps, double timeout_s);
+int qdfn_ensemble_run_async(qdfn_ensemble* ens, int64_t nsteps, double timeout_s, void* stream);
+int qdfn_ensemble_sync(qdfn_ensemble* ens);
+/* Host-only split rule used above: out[k] >= 1 blocks for member k, in
+ * proportion to cost[k] > 0, summing to at most nsm (largest remainder). */
+int qdfn_ensemble_shares(int n, const double* cost, int nsm, int* out);
 /* Cumulative device counters of the context's runs (first n of): ns spent in
  * [0] time-step control, [1] elastic operator, [2] friction solves and retries,
  * [3] state rotation; [4] solve passes (1 + retries per step), [5] steps;
@@ -251,12 +295,22 @@ int qdfn_get_kself(const qdfn_ctx* ctx, double* kself);
  * K[recv, src]: entry (r, s) at s*ld + r) and device vectors D, tld, knd (length
  * N), enqueued on `stream`.  Allocates nothing: its scratch is a fixed 2 MiB
  * device array holding N <= 16384; larger N is rejected with QDFN_ERR_INVALID.
- * The first call on each device looks up the array's device address (with that
- * device current), so make that first call before any stream capture.  All
+ * Each call made outside stream capture looks up the array's device address
+ * (with the device current) and records it; calls made during capture use the
+ * recorded one, so make the first call on each device before any capture.  All
  * calls on a device share the array: calls whose kernels overlap on the GPU
  * (other streams or host threads) race and must not be issued. */
 int qdfn_apply_dense_noalloc(int64_t N, const double* Ks, const double* Kn, int64_t ld,
                              const double* D, double* tld, double* knd, void* stream);
+
+/* ---- self-checks ------------------------------------------------------------ */
+/* The friction solves divide by Dt, Dc, a and constants through a correctly
+ * rounded reciprocal and one remainder correction (3 FP64 operations instead
+ * of a full IEEE division), falling back to IEEE division outside
+ * [2^-895, 2^896].  This evaluates that division on DEVICE arrays,
+ * q[i] = x[i] / d[i], on `stream`, so that tests can compare it with IEEE
+ * division.  No counterpart in the reference (Julia's `/`). */
+int qdfn_check_division(int64_t n, const double* x, const double* d, double* q, void* stream);
 
 /* ---- input parsing and discretisation (host only) ------------------------ */
 /* The reference's RUN2 front end, so a caller goes from the bulk text file to

@@ -1,0 +1,62 @@
+// Ensemble launch kernels: k_sim_members (several contexts in one cooperative
+// grid, sim_kernel.cuh) instantiated for every operator format and instance
+// count, plus the two small kernels around it -- clearing every member's
+// error flag and barrier arrivals before the launch, and gathering every
+// member's outcome into one array after it.  The host side (qdfn_ensemble_*)
+// is in sim.cu beside the context it drives.
+#include "ensemble_kernels.h"
+#include "sim_kernel.cuh"
+
+namespace qdfn {
+namespace {
+
+// one thread per member: error flag and barrier arrivals (adjacent words)
+__global__ void k_members_reset(const SimParams* __restrict__ members, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    members[m].gerr[0] = 0;
+    *members[m].bar_count = 0u;
+}
+
+// one thread per member: the first failing instance's status, else the
+// launch's error flag, else 0
+__global__ void k_members_status(const SimParams* __restrict__ members, int n, int* __restrict__ out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    const SimParams& p = members[m];
+    int s = 0;
+    for (int r = 0; r < p.R && s == 0; ++r) s = p.status[r];
+    if (s == 0) s = p.gerr[0];
+    out[m] = s;
+}
+
+template <class M>
+MembersKernel pick(int R) {
+    switch (R) {
+        case 1: return k_sim_members<M, 1>;
+        case 2: return k_sim_members<M, 2>;
+        default: return k_sim_members<M, 4>;
+    }
+}
+
+}  // namespace
+
+MembersKernel members_kernel(int prec, int R) {
+    if (prec == QDFN_FP64) return pick<FmtF64>(R);
+    if (prec == QDFN_FP32) return pick<FmtF32>(R);
+    return pick<FmtBF16x2>(R);
+}
+
+int members_reset(const SimParams* dmembers, int n, cudaStream_t st) {
+    k_members_reset<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n);
+    QDFN_CUDA(cudaGetLastError());
+    return QDFN_OK;
+}
+
+int members_status(const SimParams* dmembers, int n, int* dout, cudaStream_t st) {
+    k_members_status<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n, dout);
+    QDFN_CUDA(cudaGetLastError());
+    return QDFN_OK;
+}
+
+}  // namespace qdfn

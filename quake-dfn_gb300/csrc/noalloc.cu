@@ -82,18 +82,26 @@ __global__ void k_noalloc_reduce(int64_t N, int nchunk, const double* __restrict
 }
 
 // Device address of the scratch array on the current device.  The name
-// g_noalloc_scratch is a host-side stand-in, not a device address; the address
-// is looked up once per device (with that device current) and cached.
-int scratch_address(double** out) {
+// g_noalloc_scratch is a host-side stand-in, not a device address.  A call
+// made outside stream capture looks the address up (with the device current)
+// and records it for that device; a call made while `st` is being captured
+// uses the recorded address, so the first call on a device must come before
+// any capture.  Looking it up on every uncaptured call keeps the address right
+// after cudaDeviceReset, which may reload the module at another address.
+int scratch_address(cudaStream_t st, double** out) {
     int dev = 0;
     QDFN_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(QDFN_ERR_INVALID, "device index out of range");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    QDFN_CUDA(cudaStreamIsCapturing(st, &cap));
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
         g_scratch_addr[dev] = static_cast<double*>(p);
+    } else if (!g_scratch_addr[dev]) {
+        return fail(QDFN_ERR_STATE, "first call on this device made during stream capture");
     }
     *out = g_scratch_addr[dev];
     return QDFN_OK;
@@ -112,14 +120,14 @@ extern "C" int qdfn_apply_dense_noalloc(int64_t N, const double* Ks, const doubl
                                           std::to_string(kNoAllocMaxN) + " patches");
     if (ld < N) return fail(QDFN_ERR_INVALID, "ld < N");
     if (!Ks || !Kn || !D || !tld || !knd) return fail(QDFN_ERR_INVALID, "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
     double* scratch = nullptr;
-    int rc = scratch_address(&scratch);
+    int rc = scratch_address(st, &scratch);
     if (rc) return rc;
     const int64_t chunk = (N + kNoAllocChunks - 1) / kNoAllocChunks;
     const int nchunk = (int)((N + chunk - 1) / chunk);
     const int64_t rows_per_blk = (int64_t)kNoAllocThreads * 2;
     dim3 grid((unsigned)((N + rows_per_blk - 1) / rows_per_blk), (unsigned)nchunk);
-    cudaStream_t st = (cudaStream_t)stream;
     k_noalloc_chunk<<<grid, kNoAllocThreads, 0, st>>>(N, Ks, Kn, ld, D, chunk, scratch);
     QDFN_CUDA(cudaGetLastError());
     k_noalloc_reduce<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, nchunk, scratch, tld, knd);

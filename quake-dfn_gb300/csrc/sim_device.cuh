@@ -80,7 +80,7 @@ __device__ __forceinline__ Recip recip_pre(double d, double y) {
     r.ok = in_safe_range(exp_field(d));
     return r;
 }
-__device__ __noinline__ double full_div(double x, double d) { return x / d; }
+static __device__ __noinline__ double full_div(double x, double d) { return x / d; }
 __device__ __forceinline__ double div_by(double x, const Recip& R) {
     const double q0 = x * R.y;
     const double r = fma(-q0, R.d, x);
@@ -93,11 +93,11 @@ __device__ __forceinline__ double div_by(double x, const Recip& R) {
 
 // The alpha terms as written in the reference.  Out of line so that the
 // compiler cannot evaluate them speculatively next to the (usual) skip path.
-__device__ __noinline__ double alpha_term_fast(double alpha, double sig, double sig_old, double Dt,
+static __device__ __noinline__ double alpha_term_fast(double alpha, double sig, double sig_old, double Dt,
                                                double b) {
     return alpha * (sig - sig_old) / Dt / b / sig;
 }
-__device__ __noinline__ double alpha_term_slow(double alpha, double sig, double sig_old, double Dt,
+static __device__ __noinline__ double alpha_term_slow(double alpha, double sig, double sig_old, double Dt,
                                                double b) {
     return alpha * Dt * (sig - sig_old) / Dt / b / sig;
 }
@@ -159,7 +159,7 @@ __device__ __forceinline__ double evolution(double ThetaOld, double Dt, double V
         }                                                                     \
     } while (0)
 
-__device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+static __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
                                 int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;
@@ -219,7 +219,7 @@ __device__ PatchOut solve_highv(const PatchIn& p, double Dt, double eta, double 
 // count where the reference loop raises them: the update's (evolution law,
 // friction logarithms) only when the update runs (V >= 0, not NaN); the
 // second evaluation's only when the first passed.
-__device__ PatchOut solve_highv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+static __device__ PatchOut solve_highv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
                                      int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;
@@ -338,7 +338,7 @@ __device__ PatchOut solve_highv_pair(const PatchIn& p, double Dt, double eta, do
     } while (0)
 
 // One lane per patch.
-__device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+static __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double alpha, int dr,
                                double SwitchV, int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;
@@ -410,7 +410,7 @@ __device__ PatchOut solve_lowv(const PatchIn& p, double Dt, double eta, double a
 // first passed).  A lone warp issues one FP64 instruction per ~70 cycles on
 // this part, so the chain sets the solve time where few warps are left to run
 // (the last row blocks of a step).
-__device__ PatchOut solve_lowv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
+static __device__ PatchOut solve_lowv_pair(const PatchIn& p, double Dt, double eta, double alpha, int dr,
                                     double SwitchV, int& err) {
     int FLAG = 1, Instab = 0, Iteration = 0;
     double maxDiff = 10, crit = kConv;

@@ -32,6 +32,9 @@ EXPORTS = [
     "qdfn_get_state", "qdfn_set_state", "qdfn_get_history", "qdfn_apply_operator", "qdfn_get_kself",
     "qdfn_apply_dense_noalloc", "qdfn_set_state_all", "qdfn_get_state_all", "qdfn_set_blocks",
     "qdfn_get_blocks", "qdfn_read_bulk_input", "qdfn_bulk_to_segment", "qdfn_rot_verts_unit_vectors",
+    "qdfn_ensemble_create", "qdfn_ensemble_destroy", "qdfn_ensemble_get_blocks", "qdfn_ensemble_set_blocks",
+    "qdfn_ensemble_balance", "qdfn_ensemble_run", "qdfn_ensemble_run_async", "qdfn_ensemble_sync",
+    "qdfn_ensemble_shares", "qdfn_check_division",
 ]
 
 
@@ -114,6 +117,16 @@ def load():
     L.qdfn_read_bulk_input.argtypes = [C.c_char_p, C.POINTER(BulkInfo), C.c_void_p, C.c_int64]
     L.qdfn_bulk_to_segment.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
     L.qdfn_rot_verts_unit_vectors.argtypes = [C.c_int64] + [C.c_void_p] * 11
+    L.qdfn_ensemble_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), C.c_void_p]
+    L.qdfn_ensemble_destroy.argtypes = [C.c_void_p]
+    L.qdfn_ensemble_get_blocks.argtypes = [C.c_void_p, C.c_void_p]
+    L.qdfn_ensemble_set_blocks.argtypes = [C.c_void_p, C.c_void_p]
+    L.qdfn_ensemble_balance.argtypes = [C.c_void_p]
+    L.qdfn_ensemble_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]
+    L.qdfn_ensemble_run_async.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]
+    L.qdfn_ensemble_sync.argtypes = [C.c_void_p]
+    L.qdfn_ensemble_shares.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+    L.qdfn_check_division.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 

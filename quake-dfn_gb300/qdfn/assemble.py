@@ -71,3 +71,19 @@ def assemble_rect_dev(src, recv, shear_modulus, poisson, Ks, Kn, stream=0, layou
     _lib.check(L.qdfn_assemble_rect_dev(src.shape[0], src.data_ptr(), recv.shape[0], recv.data_ptr(),
                                         float(shear_modulus), float(poisson), Ks.data_ptr(), Kn.data_ptr(), ld, lay,
                                         stream))
+
+
+def assemble_tri_dev(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, Ks, Kn, stream=0, layout="col"):
+    """Device-pointer form of assemble_tri on torch tensors: P1/P2/P3
+    (n_src x 3), rake (n_src), centre/nhat/shat (n_recv x 3), all contiguous
+    float64 CUDA tensors (slices of larger ones included); Ks/Kn preallocated,
+    layout="col": shape (n_src, n_recv), entry (r, s) at s*ld + r."""
+    L = _lib.load()
+    lay = _lib.LAYOUT_COL if layout == "col" else _lib.LAYOUT_ROW
+    for t in (P1, P2, P3, rake, centre, nhat, shat):
+        if not t.is_contiguous():
+            raise ValueError("assemble_tri_dev needs contiguous tensors")
+    _lib.check(L.qdfn_assemble_tri_dev(P1.shape[0], P1.data_ptr(), P2.data_ptr(), P3.data_ptr(), rake.data_ptr(),
+                                       centre.shape[0], centre.data_ptr(), nhat.data_ptr(), shat.data_ptr(),
+                                       float(shear_modulus), float(poisson), Ks.data_ptr(), Kn.data_ptr(),
+                                       Ks.stride(0), lay, stream))

@@ -28,7 +28,9 @@ UNITS = {
     "assemble_rect.cu": ["--fmad=false"],
     "assemble_tri.cu": ["--fmad=false"],
     "sim.cu": ["--fmad=false"],
+    "ensemble.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
+    "selfcheck.cu": ["--fmad=false"],
 }
 
 

@@ -1,48 +1,45 @@
-"""Batched ensembles of geometries of uneven size on one GPU.
+"""Batched ensembles of fault networks of uneven size in one persistent launch.
 
-Each geometry (with its friction draws, up to 4 per geometry sharing the
-operator) is one qdfn context.  The contexts split the SMs in proportion to
-their work -- operator bytes per step plus the per-patch solves -- through
-``qdfn_set_blocks``, and their persistent runs are launched on separate streams,
-so every geometry advances at once on its own share of the GPU with its own
-adaptive time steps.  The contexts share nothing and never wait on one
-another.  (The reference runs one geometry per Julia process.)
+Each geometry with its friction draws (up to 4 per geometry, sharing the
+operator) is one qdfn context.  ``qdfn_ensemble_create`` groups the contexts so
+that ONE cooperative launch advances all of them: member k runs on its own
+contiguous range of thread blocks (its share of the SMs) with its own grid
+barrier and its own adaptive time steps, and the members never wait on one
+another.  The shares start from a cost estimate (operator bytes plus patch
+solves) and ``balance`` -- the autotuner -- re-divides the SMs by each member's
+measured device time, so that members taking the same number of steps finish
+together.  (The reference runs one geometry per Julia process;
+scripts/Functions_RSFDFN3DMain_D.jl:146-322 is the loop each member runs.)
 """
+import ctypes as C
+
 import numpy as np
 
-from . import simulate
+from . import _lib, simulate
 
 
-def sm_shares(work, n_sms):
-    """Blocks per member: at least one each, proportional to `work`, summing
-    to at most n_sms (members beyond n_sms cannot all be resident at once)."""
-    work = np.asarray(work, dtype=np.float64)
-    m = work.shape[0]
-    if m > n_sms:
-        raise ValueError("%d members need at least %d SMs" % (m, m))
-    share = np.maximum(1, np.floor(n_sms * work / work.sum()).astype(np.int64))
-    while share.sum() > n_sms:                       # trim the largest
-        share[np.argmax(share)] -= 1
-    spare = n_sms - int(share.sum())                 # hand out the rest by largest deficit
-    if spare > 0:
-        deficit = n_sms * work / work.sum() - share
-        for k in np.argsort(-deficit)[:spare]:
-            share[k] += 1
-    return share
+def sm_shares(cost, n_sms):
+    """Blocks per member: at least one each, in proportion to ``cost``, summing
+    to at most ``n_sms`` (largest remainder) -- the library's split rule
+    (qdfn_ensemble_shares, host code, no GPU needed)."""
+    cost = np.ascontiguousarray(np.asarray(cost, dtype=np.float64))
+    out = np.zeros(cost.shape[0], dtype=np.int32)
+    _lib.check(_lib.load().qdfn_ensemble_shares(int(cost.shape[0]), C.c_void_p(cost.ctypes.data), int(n_sms),
+                                                C.c_void_p(out.ctypes.data)))
+    return out.astype(np.int64)
 
 
 class Ensemble:
     """members: list of dicts with keys ``problem`` (as for simulate.Simulation,
     per-patch arrays of length n_inst*N), ``n_inst``, ``Ks``/``Kn`` (host
-    arrays or float64 CUDA tensors in column layout, see set_dense_device),
-    optional ``ext`` (dict t/normal/shear/pressure).  precision as for
-    Simulation.set_dense."""
+    arrays, or float64 CUDA tensors in column layout), optional ``ext`` (dict
+    t/normal/shear/pressure), ``record_step``/``max_records``.  precision as
+    for Simulation.set_dense.  blocks: per-member block counts, or None for the
+    library's cost estimate."""
 
-    def __init__(self, members, precision="fp32", n_sms=None):
-        import torch
+    def __init__(self, members, precision="fp32", blocks=None):
+        self.L = _lib.load()
         self.members = []
-        self.streams = []
-        work = []
         for m in members:
             sim = simulate.Simulation(m["problem"], n_inst=m.get("n_inst", 1),
                                       record_step=m.get("record_step", 0), max_records=m.get("max_records", 0))
@@ -53,34 +50,58 @@ class Ensemble:
             if m.get("ext") is not None:
                 e = m["ext"]
                 sim.set_external_stress(e["t"], e["normal"], e["shear"], e["pressure"])
-            N, R = sim.N, sim.n_inst
-            work.append(float(N) * N * 2 * (8 if precision == "fp64" else 4) + 2000.0 * N * R)
             self.members.append(sim)
-            self.streams.append(torch.cuda.Stream())
-        if n_sms is None:
-            n_sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-        self.blocks = sm_shares(work, n_sms)
-        for sim, b in zip(self.members, self.blocks):
-            sim.set_blocks(int(b))
+        n = len(self.members)
+        handles = (C.c_void_p * n)(*[s._h.value for s in self.members])
+        bl = None
+        if blocks is not None:
+            bl = np.ascontiguousarray(np.asarray(blocks, dtype=np.int32))
+            if bl.shape[0] != n:
+                raise ValueError("blocks: expected %d values" % n)
+        h = C.c_void_p()
+        _lib.check(self.L.qdfn_ensemble_create(C.byref(h), n, handles,
+                                               None if bl is None else C.c_void_p(bl.ctypes.data)))
+        self._h = h
 
-    def run_async(self, nsteps, timeout_s=0.0):
-        for sim, st in zip(self.members, self.streams):
-            sim.run_async(nsteps, stream=st.cuda_stream, timeout_s=timeout_s)
+    @property
+    def blocks(self):
+        out = np.zeros(len(self.members), dtype=np.int32)
+        _lib.check(self.L.qdfn_ensemble_get_blocks(self._h, C.c_void_p(out.ctypes.data)))
+        return out
+
+    def set_blocks(self, blocks=None):
+        bl = None if blocks is None else np.ascontiguousarray(np.asarray(blocks, dtype=np.int32))
+        _lib.check(self.L.qdfn_ensemble_set_blocks(self._h, None if bl is None else C.c_void_p(bl.ctypes.data)))
+
+    def balance(self):
+        """Autotuner step: re-divide the SMs by the members' measured cost since
+        the last balance."""
+        _lib.check(self.L.qdfn_ensemble_balance(self._h))
+
+    def autotune(self, steps, rounds=3, timeout_s=0.0):
+        """Runs `steps` steps in `rounds` parts with a balance after each (these
+        steps advance the ensemble: use them as warm-up).  Returns the shares
+        after each round."""
+        hist = [self.blocks.copy()]
+        per = max(1, int(steps) // max(1, int(rounds)))
+        done = 0
+        while done < steps:
+            n = min(per, steps - done)
+            self.run(n, timeout_s=timeout_s)
+            done += n
+            self.balance()
+            hist.append(self.blocks.copy())
+        return hist
+
+    def run_async(self, nsteps, timeout_s=0.0, stream=None):
+        _lib.check(self.L.qdfn_ensemble_run_async(self._h, int(nsteps), float(timeout_s),
+                                                  C.c_void_p(stream) if stream else None))
 
     def sync(self):
-        """Waits for every member; raises the first member's error."""
-        err = None
-        for sim in self.members:
-            try:
-                sim.sync()
-            except Exception as e:   # keep draining the others
-                err = err or e
-        if err is not None:
-            raise err
+        _lib.check(self.L.qdfn_ensemble_sync(self._h))
 
     def run(self, nsteps, timeout_s=0.0):
-        self.run_async(nsteps, timeout_s)
-        self.sync()
+        _lib.check(self.L.qdfn_ensemble_run(self._h, int(nsteps), float(timeout_s)))
 
     def sim_years(self):
         """Simulated time of every instance of every member, in years."""
@@ -88,3 +109,17 @@ class Ensemble:
         for sim in self.members:
             out.extend(sim.state(r)["T"] / (365.25 * 86400.0) for r in range(sim.n_inst))
         return np.asarray(out)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.L.qdfn_ensemble_destroy(self._h)
+            self._h = None
+        for s in self.members:
+            s.close()
+        self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -225,6 +225,77 @@ def rot_verts_unit_vectors(seg, rake):
     return P1, P2, P3, un, us, ud, uslip
 
 
+def read_obj_mesh(path):
+    """Vertices and triangular faces of a Wavefront .obj mesh, read as
+    Tools/TriangleMeshReader/ObjReader.jl:44-70 reads them: `v x y z` rows
+    (extra colour columns ignored), `f a b c` rows whose entries may be
+    `i/t/n` (the first index is kept, 1-based in the file; returned 0-based);
+    other rows are skipped."""
+    verts, faces = [], []
+    with open(path) as f:
+        for line in f:
+            tok = line.split()
+            if not tok:
+                continue
+            if tok[0] == "v":
+                verts.append([float(t) for t in tok[1:4]])
+            elif tok[0] == "f":
+                if len(tok) != 4:
+                    raise InputFormatError("only triangular faces are supported")
+                faces.append([int(t.split("/")[0]) - 1 for t in tok[1:4]])
+    V = np.asarray(verts, dtype=np.float64).reshape(-1, 3)
+    F = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+    if F.size and (F.min() < 0 or F.max() >= V.shape[0]):
+        raise InputFormatError("face index out of range")
+    return V, F
+
+
+# ObjReader.jl:17-38 defaults: the bulk header and the per-triangle properties
+OBJ_DEFAULTS = dict(switch_ss_rn=0, shear_modulus=20e9, poisson=0.25, rock_density=2670.0, crit_too_close=1.05,
+                    too_close_normal_multiplier=0.6, min_normal_stress=2e6, amp=100.0, rake=0.0, a=0.005, b=0.01,
+                    Dc=1e-3, theta_i=1e5, V_i=1e-15, friction_i=0.6, normal_stress_surface=10e6,
+                    normal_stress_gradient=0.0, V_const=0.0, min_segment_length=100000.0)
+
+
+def obj_to_bulk(V, F, **kw):
+    """The 20-column triangle bulk table and its header line that ObjReader.jl
+    writes (:106-135): vertices scaled by `amp`, then P1, P2, P3, rake, a, b,
+    Dc, Theta_i, V_i, Friction_i, normal stress at the surface, its gradient,
+    V_const and the minimum segment length per triangle."""
+    o = dict(OBJ_DEFAULTS, **kw)
+    Vs = V * o["amp"]
+    n = F.shape[0]
+    bulk = np.zeros((n, 20))
+    bulk[:, 0:3] = Vs[F[:, 0]]
+    bulk[:, 3:6] = Vs[F[:, 1]]
+    bulk[:, 6:9] = Vs[F[:, 2]]
+    bulk[:, 9] = o["rake"]
+    for col, key in ((10, "a"), (11, "b"), (12, "Dc"), (13, "theta_i"), (14, "V_i"), (15, "friction_i"),
+                     (16, "normal_stress_surface"), (17, "normal_stress_gradient"), (18, "V_const"),
+                     (19, "min_segment_length")):
+        bulk[:, col] = o[key]
+    header = [o["switch_ss_rn"], o["shear_modulus"], o["poisson"], o["rock_density"], o["crit_too_close"],
+              o["too_close_normal_multiplier"], o["min_normal_stress"]]
+    return header, bulk
+
+
+def write_bulk_file(path, header, bulk):
+    """Writes a bulk geometry file in the layout ReadBulkInput reads: a header
+    line, the seven run parameters, a column-name line, then one row per bulk
+    fault (18 columns for rectangles, 20 for triangles), tab-separated."""
+    names = ("SwitchSS/RN\tShearMod\tPoissonRatio\tR_Density\tCrit_TooClose\tTooCloseNormal_Multiplier\t"
+             "Minimum_NS")
+    cols = ("P1_x P1_y P1_z P2_x P2_y P2_z P3_x P3_y P3_z Rake a b Dc Theta_i V_i Fric_i Sig0 SigGrad V_Const "
+            "MaxLeng" if bulk.shape[1] == 20 else
+            "Ctr_X Ctr_Y Ctr_Z St_L Dip_L StAng DipAng LR/RN a b Dc Theta_i V_i Fric_i Sig0 SigGrad V_Const MaxLeng")
+    with open(path, "w") as f:
+        f.write(names + "\n")
+        f.write("\t".join(repr(float(x)) for x in header) + "\n")
+        f.write("\t".join(cols.split()) + "\n")
+        for row in bulk:
+            f.write("\t".join(repr(float(x)) for x in row) + "\n")
+
+
 def fault_mass(length_strike, length_dip, rho, vertical_length_scale=0.0):
     """FaultMass = VertScale * rho / 2 (QUAKEDFN_RunARG.jl:159-164)."""
     if vertical_length_scale == 0:

@@ -93,15 +93,24 @@ def aca(block, tol, max_rank=None):
     """ACA with partial pivoting on a dense torch block (m x n), then QR/SVD
     recompression; returns (U (m x k), Vt (k x n)) with
     ||block - U Vt||_F <= tol ||block||_F (estimated the ACA way)."""
-    import torch
     m, n = block.shape
+    return aca_fn(lambda i: block[i].clone(), lambda j: block[:, j].clone(), m, n, tol, max_rank,
+                  device=block.device, dtype=block.dtype)
+
+
+def aca_fn(row_fn, col_fn, m, n, tol, max_rank=None, device=None, dtype=None):
+    """ACA with partial pivoting (Bebendorf's rule) on a block known only through
+    row_fn(i) -> row i (length n) and col_fn(j) -> column j (length m), torch
+    tensors; then QR/SVD recompression.  Entries are formed on demand -- a rank-k
+    block costs about k (m + n) evaluations instead of m n."""
+    import torch
     max_rank = max_rank or min(m, n)
     Us, Vs = [], []
-    used_rows = torch.zeros(m, dtype=torch.bool, device=block.device)
+    used_rows = torch.zeros(m, dtype=torch.bool, device=device)
     i = 0
     frob2 = 0.0
     for _ in range(max_rank):
-        row = block[i].clone()
+        row = row_fn(i)
         for u, v in zip(Us, Vs):
             row -= u[i] * v
         used_rows[i] = True
@@ -114,7 +123,7 @@ def aca(block, tol, max_rank=None):
             i = int(cand[0])
             continue
         v = row / piv
-        col = block[:, j].clone()
+        col = col_fn(j)
         for u, vv in zip(Us, Vs):
             col -= vv[j] * u
         u = col
@@ -132,8 +141,8 @@ def aca(block, tol, max_rank=None):
         if cand[i] < 0:
             break
     if not Us:
-        return (torch.zeros((m, 0), dtype=block.dtype, device=block.device),
-                torch.zeros((0, n), dtype=block.dtype, device=block.device))
+        return (torch.zeros((m, 0), dtype=dtype, device=device),
+                torch.zeros((0, n), dtype=dtype, device=device))
     U = torch.stack(Us, dim=1)
     V = torch.stack(Vs, dim=0)
     # recompression: U = Qu Ru, V^T = Qv Rv -> SVD of Ru Rv^T
@@ -208,6 +217,57 @@ def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, devi
                     Ul.append(None); Vl.append(None); Dl.append(B.cpu().numpy())
         else:
             for B, Ul, Vl, Dl in ((Bs, us, vs, ds), (Bn, un, vn, dn)):
+                Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
+    return HMatrix(np.array(ranges, dtype=np.int64), ds, us, vs, dn, un, vn, perm), perm
+
+
+def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6,
+              device="cuda"):
+    """Build the H-matrix of a triangular-patch system (TDstressHS kernels,
+    StiffnessMatrix_ByParts_Calculation_Tri, scripts/Functions_BuildInputFile.jl:551-594,
+    in the block structure HmatBuild_T builds at :643-723).  Near-field blocks
+    are assembled densely on the GPU; admissible blocks are compressed by ACA
+    whose rows and columns are single receivers x a source range and a receiver
+    range x single sources of the assembly kernel -- no admissible block is ever
+    formed whole.  Returns (HMatrix, perm): block ranges index the permuted
+    ordering (every per-patch array [perm])."""
+    import torch
+    from . import assemble
+    tree = ClusterTree(np.asarray(centre), leaf=leaf)
+    perm = tree.perm
+    dv = lambda a: torch.tensor(np.ascontiguousarray(np.asarray(a)[perm]), dtype=torch.float64,
+                                device=device)
+    p1, p2, p3, rk, cen, nh, sh = (dv(a) for a in (P1, P2, P3, rake, centre, nhat, shat))
+    G, nu = shear_modulus, poisson
+
+    def block(s0, s1, r0, r1):
+        """(Ks, Kn) of receivers [r0, r1) x sources [s0, s1), each (recv x src)."""
+        ns, nr = s1 - s0, r1 - r0
+        Ks = torch.empty((ns, nr), dtype=torch.float64, device=device)
+        Kn = torch.empty((ns, nr), dtype=torch.float64, device=device)
+        assemble.assemble_tri_dev(p1[s0:s1], p2[s0:s1], p3[s0:s1], rk[s0:s1], cen[r0:r1], nh[r0:r1], sh[r0:r1],
+                                  G, nu, Ks, Kn, layout="col")
+        return Ks.T, Kn.T
+
+    ranges, ds, us, vs, dn, un, vn = [], [], [], [], [], [], []
+    for (s, t, adm) in block_partition(tree, eta):
+        s0, s1 = tree.starts[s], tree.ends[s]
+        r0, r1 = tree.starts[t], tree.ends[t]
+        ns, nr = s1 - s0, r1 - r0
+        ranges.append((s0, s1 - 1, r0, r1 - 1))
+        if not adm:
+            Bs, Bn = block(s0, s1, r0, r1)
+            for B, Ul, Vl, Dl in ((Bs, us, vs, ds), (Bn, un, vn, dn)):
+                Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
+            continue
+        for side, (Ul, Vl, Dl) in enumerate(((us, vs, ds), (un, vn, dn))):
+            row = lambda i: block(s0, s1, r0 + i, r0 + i + 1)[side][0].clone()
+            col = lambda j: block(s0 + j, s0 + j + 1, r0, r1)[side][:, 0].clone()
+            U, Vt = aca_fn(row, col, nr, ns, tol, device=device, dtype=torch.float64)
+            if U.shape[1] * (nr + ns) < nr * ns:
+                Ul.append(U.cpu().numpy()); Vl.append(Vt.cpu().numpy()); Dl.append(None)
+            else:
+                B = block(s0, s1, r0, r1)[side]
                 Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
     return HMatrix(np.array(ranges, dtype=np.int64), ds, us, vs, dn, un, vn, perm), perm
 

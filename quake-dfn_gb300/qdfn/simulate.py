@@ -224,17 +224,36 @@ def _load_external_stress(N):
                 shear=z["ExternalStress_Shear"], pressure=z["Pressure"])
 
 
+def _padded(a, rows):
+    """History array padded with zero rows to the reference's TotalRecord rows
+    (Main_D :133-141 allocates zeros(TotalRecord, N) and fills record by record)."""
+    a = np.asarray(a)
+    if a.ndim == 1:
+        a = a.reshape(-1, 1)
+    out = np.zeros((rows, a.shape[1]))
+    n = min(rows, a.shape[0])
+    out[:n] = a[:n]
+    return out
+
+
 def _run_and_save(sim, TotalStep, RecordStep, SaveStep, SaveResultFileName, verbose):
+    """Runs TotalStep steps in SaveStep chunks and saves the history after every
+    chunk that ends on a multiple of SaveStep, as Main_D :286-290 does (with
+    SaveStep <= 0: one chunk, saved at its end).  The saved arrays have
+    TotalRecord = round(TotalStep / RecordStep) rows, zero past the records
+    written so far, like the reference's; History_Dt is saved beside them."""
     done = 0
     chunk = int(SaveStep) if SaveStep and SaveStep > 0 else int(TotalStep)
+    rows = int(round(TotalStep / RecordStep)) if RecordStep else 0
     while done < TotalStep:
         n = min(chunk, TotalStep - done)
         sim.run(n)
         done += n
         h = sim.history(0)
-        if SaveResultFileName:
-            np.savez(SaveResultFileName, History_V=h["V"], History_Disp=h["D"], History_Time=h["T"].reshape(-1, 1),
-                     History_Theta=h["theta"], History_NormalStress=h["sigma"], History_Dt=h["Dt"].reshape(-1, 1))
+        if SaveResultFileName and (done % chunk == 0 or not (SaveStep and SaveStep > 0)):
+            np.savez(SaveResultFileName, History_V=_padded(h["V"], rows), History_Disp=_padded(h["D"], rows),
+                     History_Time=_padded(h["T"], rows), History_Theta=_padded(h["theta"], rows),
+                     History_NormalStress=_padded(h["sigma"], rows), History_Dt=_padded(h["Dt"], rows))
         if verbose:
             st = sim.state(0)
             print("%.5f %.5f   %.3e   %.3e" % (done / TotalStep, st["T"] / 86400, np.max(st["V"]), st["dt"]))

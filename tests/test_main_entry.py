@@ -74,7 +74,28 @@ def test_main_maps_the_reference_arguments(monkeypatch, tmp_path):
     assert sorted(z.files) == sorted(["History_V", "History_Disp", "History_Time", "History_Theta",
                                       "History_NormalStress", "History_Dt"])
     assert z["History_V"].shape == (10, N) and z["History_Time"].shape == (10, 1)
+    # saved at step 90, the last multiple of SaveStep (Main_D :286): 9 records,
+    # the 10th row still the zeros the reference allocates
+    assert np.all(z["History_V"][:9] == 1.0) and np.all(z["History_V"][9] == 0.0)
+    assert z["History_Time"][8, 0] == 90.0 and z["History_Time"][9, 0] == 0.0
     assert hist["T"].shape == (10,)
+
+
+def test_saved_history_is_padded_to_total_record(monkeypatch, tmp_path):
+    """Every save holds TotalRecord x N arrays (Main_D :133-141, 287-289),
+    zero past the records written so far."""
+    monkeypatch.setattr(simulate, "Simulation", FakeSimulation)
+    N = 5
+    Ks, Kn = np.eye(N) * -1e9, np.eye(N) * 2e8
+    out = str(tmp_path / "res.npz")
+    simulate.main(*_args(N, Ks, Kn, total=100, record=10, save_step=50, out=out), external_stress=None)
+    z = np.load(out)                      # last save at step 100: all 10 records
+    for k in ("History_V", "History_Disp", "History_Theta", "History_NormalStress"):
+        assert z[k].shape == (10, N), k
+    assert z["History_Time"].shape == (10, 1) and z["History_Time"][9, 0] == 100.0
+    simulate.main(*_args(N, Ks, Kn, total=100, record=10, save_step=50, out=out), external_stress=None)
+    sim = FakeSimulation.made[-1]
+    assert sim.runs == [50, 50]
 
 
 def test_main_zero_normal_and_external_stress_file(monkeypatch, tmp_path):

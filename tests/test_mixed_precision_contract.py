@@ -1,0 +1,132 @@
+"""The mixed-precision contract against the FP64 oracle: with the elastic
+operator stored in FP32 (FP64 state, friction inversion, time and step
+control), the relative slip error max|D - D_oracle| / max|D_oracle| stays at
+or below 1e-6, and simulated time within 1e-6, at every recorded step of the
+horizon before the first event.  Past the first event (a patch on the
+high-velocity solver, V > SwitchV) the trajectories are chaotic: a 1e-15
+perturbation of the FP64 operator already grows to ~1e-6 within a few hundred
+steps there, so the contract is stated over the pre-event horizon, which each
+test measures from the oracle's own run and requires to be long.
+
+Runs: the C1 single fault (the dense FP32 product, one instance), a reduced C2
+network (dense FP32, 4 friction draws in one context), and the same network as
+an H-matrix (FP32 blocks against the oracle's FP64 H product).  The BF16 hi+lo
+operator (~16 significant bits) is held to its own, stated bound."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+G, NU = 32e9, 0.25
+
+
+def pre_event_records(hist, ns, switch_v):
+    """Leading records with no patch above SwitchV (nothing on the
+    high-velocity solver yet)."""
+    vmax = np.max(hist["V"][:, :ns], axis=1)
+    bad = np.nonzero(vmax > switch_v)[0]
+    return int(bad[0]) if bad.size else int(vmax.shape[0])
+
+
+def _compare(gh, oh, n):
+    """Relative slip error and relative time error over the first n records."""
+    d = float(np.max(np.abs(gh["D"][:n] - oh["D"][:n])) / max(np.max(np.abs(oh["D"][:n])), 1e-300))
+    t = float(np.max(np.abs(gh["T"][:n] / oh["T"][:n] - 1)))
+    return d, t
+
+
+def _oracle(oracle_mod, prob, ext, op, nsteps, rstep, r=None):
+    p = dict(prob, ext_t=ext["t"], ext_n=ext["normal"], ext_s=ext["shear"], ext_p=ext["pressure"])
+    if r is not None:
+        N = prob["N"]
+        for k in ("a", "b", "Dc", "theta_i", "V_i", "f_i"):
+            p[k] = np.asarray(prob[k])[r * N:(r + 1) * N]
+        for k in ("sigma0", "V_const", "mass"):
+            p[k] = np.asarray(prob[k])[:N]
+    o = oracle_mod.Simulation(p, op)
+    return o.run(nsteps, record_step=rstep, max_rec=nsteps // rstep)
+
+
+def test_c1_single_fault_fp32_within_1e6_of_the_oracle(qdfn_mod, oracle_mod):
+    from qdfn import assemble, simulate, synth
+    sysd = synth.single_fault()
+    rec = sysd["records"]
+    Ks, Kn = assemble.assemble_rect(rec, rec, sysd["G"], sysd["nu"])
+    prob = synth.problem_dict(sysd, np.diag(Ks))
+    ext = synth.external_ramp(sysd["N"], sysd["stressing_rate"], 1e12)
+    steps, rstep = 300, 2
+    oh = _oracle(oracle_mod, prob, ext, ("dense", Ks, Kn), steps, rstep)
+    n = pre_event_records(oh, sysd["N"], prob["switch_v"])
+    assert n * rstep >= 100                     # the first event nucleates near step 150
+    sim = simulate.Simulation(prob, record_step=rstep, max_records=steps // rstep)
+    sim.set_dense(Ks, Kn, "fp32")
+    sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+    sim.run(steps, timeout_s=120)
+    d, t = _compare(sim.history(0), oh, n)
+    assert d <= 1e-6 and t <= 1e-6, (d, t, n)
+    sim.close()
+
+
+def _network(seed=2, n_faults=6, patch=100.0):
+    from qdfn import assemble, synth
+    sysd = synth.fault_network(seed=seed, n_faults=n_faults, patch=patch)
+    rec = sysd["records"]
+    Ks, Kn = assemble.assemble_rect(rec, rec, sysd["G"], sysd["nu"])
+    draws = synth.friction_draws(sysd, 4, seed=1)
+    prob = synth.problem_dict(sysd, np.diag(Ks), n_inst=4, draws=draws)
+    ext = synth.external_ramp(sysd["N"], sysd["stressing_rate"], 1e12)
+    return sysd, rec, Ks, Kn, prob, ext
+
+
+@pytest.mark.parametrize("precision,bound", [("fp32", 1e-6), ("bf16x2", 5e-5)])
+def test_reduced_network_four_draws_within_bound_of_the_oracle(qdfn_mod, oracle_mod, precision, bound):
+    """A reduced C2 network (6 faults of the C2 distributions, 100 m patches)
+    with 4 friction draws in one context, 400 steps: every draw against its own
+    FP64 oracle run over its pre-event horizon.  FP32: 1e-6 (the contract).
+    BF16 hi+lo: 5e-5 (its ~16 significant bits; not the contract's format)."""
+    from qdfn import simulate
+    sysd, rec, Ks, Kn, prob, ext = _network()
+    N = sysd["N"]
+    steps, rstep = 400, 5
+    sim = simulate.Simulation(prob, n_inst=4, record_step=rstep, max_records=steps // rstep)
+    sim.set_dense(Ks, Kn, precision)
+    sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+    sim.run(steps, timeout_s=120)
+    worst, horizons = 0.0, []
+    for r in range(4):
+        oh = _oracle(oracle_mod, prob, ext, ("dense", Ks, Kn), steps, rstep, r=r)
+        n = pre_event_records(oh, N - sysd["Nload"], prob["switch_v"])
+        horizons.append(n * rstep)
+        if n:
+            d, t = _compare(sim.history(r), oh, n)
+            worst = max(worst, d, t)
+    assert sorted(horizons)[1] >= 100, horizons       # at least three draws compared over >= 100 steps
+    assert worst <= bound, (worst, horizons)
+    sim.close()
+
+
+def test_hmatrix_fp32_within_1e6_of_the_oracle_h_product(qdfn_mod, oracle_mod):
+    """The same kind of network through the H-matrix path (ACA blocks at
+    1e-8): FP32 block storage on the GPU against the oracle's FP64 product of
+    the same blocks, 300 steps, pre-event horizon."""
+    from qdfn import hmatrix, simulate, synth
+    from _systems import problem_for, small_network
+    sysd = small_network(seed=5, n_faults=6, patch=250.0)
+    rec = sysd["records"]
+    H, perm = hmatrix.build_rect(rec, G, NU, leaf=32, eta=2.0, tol=1e-8)
+    recp = rec[perm]
+    Hs, _ = H.to_dense(rec.shape[0])
+    prob = problem_for(recp, Hs, seed=3)
+    prob["interp_at_told"] = 1
+    ext = synth.external_ramp(rec.shape[0], 1e6, 1e11)
+    steps, rstep = 300, 5
+    blocks = dict(range=H.ranges, sD=H.dense_s, sU=H.U_s, sVt=H.Vt_s, nD=H.dense_n, nU=H.U_n, nVt=H.Vt_n)
+    oh = _oracle(oracle_mod, prob, ext, ("hmat", blocks), steps, rstep)
+    n = pre_event_records(oh, rec.shape[0], prob["switch_v"])
+    assert n * rstep >= 100
+    sim = simulate.Simulation(prob, record_step=rstep, max_records=steps // rstep)
+    hmatrix.set_hmatrix(sim, H, "fp32")
+    sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+    sim.run(steps, timeout_s=120)
+    d, t = _compare(sim.history(0), oh, n)
+    assert d <= 1e-6 and t <= 1e-6, (d, t, n)
+    sim.close()
