@@ -226,10 +226,17 @@ int qdfn_ensemble_balance(qdfn_ensemble* ens);
  * `stream`; qdfn_ensemble_sync waits and returns the first failing member's
  * status. */
 int qdfn_ensemble_run(qdfn_ensemble* ens, int64_t nsteps, double timeout_s);
+/* Fill mode (off by default): in a run of nsteps, a member that has taken its
+ * nsteps keeps stepping until every member has taken at least nsteps, so no SM
+ * idles while the slowest member finishes; members then hold nsteps or more
+ * steps each (read their step counts back).  The extra steps are ordinary
+ * steps of each member's own trajectory. */
+int qdfn_ensemble_set_fill(qdfn_ensemble* ens, int on);
 int qdfn_ensemble_run_async(qdfn_ensemble* ens, int64_t nsteps, double timeout_s, void* stream);
 int qdfn_ensemble_sync(qdfn_ensemble* ens);
-/* Host-only split rule used above: out[k] >= 1 blocks for member k, in
- * proportion to cost[k] > 0, summing to at most nsm (largest remainder). */
+/* Host-only split rule used above: with member k taking cost[k] / b on b
+ * blocks, out[k] >= 1 blocks minimising the longest member time, summing to
+ * nsm (cost[k] > 0, n <= nsm). */
 int qdfn_ensemble_shares(int n, const double* cost, int nsm, int* out);
 /* Cumulative device counters of the context's runs (first n of): ns spent in
  * [0] time-step control, [1] elastic operator, [2] friction solves and retries,
@@ -284,6 +291,33 @@ int qdfn_apply_operator(qdfn_ctx* ctx, const double* D, double* tld, double* knd
 
 /* K_Self of the stored operator (length N). */
 int qdfn_get_kself(const qdfn_ctx* ctx, double* kself);
+
+/* ---- adjoint ----------------------------------------------------------------- */
+/* Reverse-mode gradient of a loss on the trajectory with respect to the
+ * per-patch friction parameters a, b and Dc.  The reference has no derivatives;
+ * this differentiates its step map (scripts/Functions_Solvers.jl:185-327 and
+ * :26-182, the products at scripts/Functions_RSFDFN3DMain_D.jl:199-202 and the
+ * time-step control at :162-201).
+ *
+ * Runs nsteps steps from the context's current state (one step per launch,
+ * checkpointing the state every checkpoint_every steps; 0 = ceil(sqrt(nsteps))),
+ * then sweeps them backwards: per step the implicit-function derivative of each
+ * patch's converged solve, the transposed products E^T and Kn^T over the stored
+ * operator (its precision), and the time step's derivative through the patch
+ * that set it.  The context ends at the window's last state, as after qdfn_run.
+ *
+ * The loss enters through its derivatives: dL_dD_final ([n_inst][N], may be
+ * NULL) on the slip after the last step, and n_seeds sparse terms on any state
+ * of the window -- seed k adds seed_dV[k] and seed_dD[k] to the adjoint of
+ * V and D of patch seed_patch[k] (-1: none) of instance seed_inst[k], and
+ * seed_dT[k] to that of its time T, after step seed_step[k] (0 = the starting
+ * state, nsteps = the last), e.g. the derivatives of an event onset time
+ * interpolated between two steps.  Outputs dL_da, dL_db, dL_dDc are
+ * [n_inst][N] host arrays.  Needs a dense operator and Alpha_Evo = 0. */
+int qdfn_adjoint_run(qdfn_ctx* ctx, int64_t nsteps, int64_t checkpoint_every, const double* dL_dD_final,
+                     int64_t n_seeds, const int64_t* seed_step, const int32_t* seed_inst,
+                     const int64_t* seed_patch, const double* seed_dV, const double* seed_dD,
+                     const double* seed_dT, double* dL_da, double* dL_db, double* dL_dDc, double timeout_s);
 
 /* ---- allocation-free operator -------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -10,9 +10,11 @@
 namespace qdfn {
 namespace {
 
-// one thread per member: error flag and barrier arrivals (adjacent words)
-__global__ void k_members_reset(const SimParams* __restrict__ members, int n) {
+// one thread per member: error flag and barrier arrivals (adjacent words);
+// thread 0 also clears the fill-mode counter
+__global__ void k_members_reset(const SimParams* __restrict__ members, int n, unsigned* fill) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m == 0 && fill) *fill = 0u;
     if (m >= n) return;
     members[m].gerr[0] = 0;
     *members[m].bar_count = 0u;
@@ -47,8 +49,8 @@ MembersKernel members_kernel(int prec, int R) {
     return pick<FmtBF16x2>(R);
 }
 
-int members_reset(const SimParams* dmembers, int n, cudaStream_t st) {
-    k_members_reset<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n);
+int members_reset(const SimParams* dmembers, int n, unsigned* dfill, cudaStream_t st) {
+    k_members_reset<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n, dfill);
     QDFN_CUDA(cudaGetLastError());
     return QDFN_OK;
 }

@@ -14,8 +14,9 @@ struct SimParams;   // sim_kernel.cuh
 using MembersKernel = void (*)(const SimParams*, const int2*, int64_t);
 MembersKernel members_kernel(int prec, int R);
 
-// clears every member's error flag and barrier arrivals (enqueued on st)
-int members_reset(const SimParams* dmembers, int n, cudaStream_t st);
+// clears every member's error flag and barrier arrivals, and the fill-mode
+// counter when dfill is not null (enqueued on st)
+int members_reset(const SimParams* dmembers, int n, unsigned* dfill, cudaStream_t st);
 // writes every member's outcome (first failing instance status, else the
 // launch's error flag, else 0) to dout[n] (enqueued on st)
 int members_status(const SimParams* dmembers, int n, int* dout, cudaStream_t st);

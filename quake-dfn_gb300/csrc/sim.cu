@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint_kernels.h"
 #include "ensemble_kernels.h"
 #include "sim_kernel.cuh"
 
@@ -45,6 +46,8 @@ struct qdfn_ctx {
     // device buffers
     std::vector<void*> allocs;
     double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega, *kself;
+    double *la = nullptr, *lth0 = nullptr;   // ln(V_i/V0), ln(theta_i V0/Dc): F0's derivatives (adjoint)
+    unsigned char* sw_used = nullptr;         // adjoint recording: solver of each patch in the next launch
     double *ra = nullptr, *rDc = nullptr;
     unsigned char* unstable;
     int* has_unstable;
@@ -127,6 +130,7 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     SimParams p{};
     p.N = c->N; p.Nload = c->Nload; p.ld = c->ld; p.R = kernel_R(c->R);
     p.nblk = c->nblocks;
+    p.sw_used = c->sw_used;
     p.evolution_dr = c->prob.evolution_dr; p.interp_at_told = c->prob.interp_at_told; p.hmat = c->hmat;
     p.eta = c->eta; p.sigma_min = c->prob.sigma_min; p.switch_v = c->prob.switch_v;
     p.dt_cut = c->prob.dt_cut; p.rupture_dt = c->prob.rupture_dt; p.max_dt = c->prob.max_dt;
@@ -327,6 +331,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(a, RN); A(b, RN); A(Dc, RN); A(F0, RN); A(tau0, RN); A(sigma0, RN); A(Vconst, RN);
     A(ra, RN); A(rDc, RN);
     A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
+    A(la, RN); A(lth0, RN);
     // the six host-visible state fields in one block, in the order of the
     // state-transfer calls, so that contiguous host buffers move in one copy
     double* state6 = nullptr;
@@ -364,6 +369,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     std::vector<double> ha(RN), hb(RN), hDc(RN), hF0(RN), htau0(RN), hs0(RN), hVc(RN), hm(RN),
         hth(RN), hV(RN), hf(RN), hzero(RN, 0.0);
     std::vector<unsigned char> hun(RN);
+    std::vector<double> hla(RN), hlth(RN);
     std::vector<int> hhas(Rk, 0);
     for (int r = 0; r < Rk; ++r) {
         const int src = r < c->R ? r : 0;
@@ -376,6 +382,8 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
                 delete c;
                 return fail(QDFN_ERR_DOMAIN, "log of a negative number in Friction0");
             }
+            hla[q] = std::log(pr->V_i[s] / sim::kV0);
+            hlth[q] = std::log(pr->theta_i[s] * sim::kV0 / pr->Dc[s]);
             hF0[q] = pr->f_i[s] - pr->a[s] * std::log(pr->V_i[s] / sim::kV0) -
                      pr->b[s] * std::log(pr->theta_i[s] * sim::kV0 / pr->Dc[s]);
             htau0[q] = pr->sigma0[s] * pr->f_i[s];
@@ -401,7 +409,8 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
         (rc = h2d(c->D, hzero.data(), RN * 8)) || (rc = h2d(c->accel, hzero.data(), RN * 8)) ||
         (rc = h2d(c->T, zeros.data(), Rk * 8)) || (rc = h2d(c->dt, ones.data(), Rk * 8)) ||
         (rc = h2d(c->step, z64.data(), Rk * 8)) || (rc = h2d(c->nrec, z64.data(), Rk * 8)) ||
-        (rc = h2d(c->status, z32.data(), Rk * 4))) {
+        (rc = h2d(c->status, z32.data(), Rk * 4)) || (rc = h2d(c->la, hla.data(), RN * 8)) ||
+        (rc = h2d(c->lth0, hlth.data(), RN * 8))) {
         delete c;
         return rc;
     }
@@ -573,6 +582,303 @@ extern "C" int qdfn_run(qdfn_ctx* c, int64_t nsteps, double timeout_s) {
 }
 
 extern "C" int qdfn_kernels_per_run(const qdfn_ctx* c) { return c ? 1 : 0; }
+// ===========================================================================
+// Adjoint of the stepped system (no counterpart in the reference, which has
+// no derivatives): the reverse-mode gradient of a loss on the trajectory with
+// respect to the per-patch a, b and Dc.
+//
+// The forward window runs one step per launch and keeps the state every
+// `cp` steps (checkpoints, cp ~ sqrt(nsteps) by default).  The reverse sweep
+// takes the segments last to first: it restores the segment's checkpoint,
+// replays its steps one per launch recording each step's state, TLD, sigma
+// and solver (the tape), and walks the tape backwards.  Per step: the
+// per-patch vector-Jacobian products of the converged solves (adjoint.cuh,
+// FP64 dual numbers), the transposed stiffness products E^T and Kn^T over the
+// stored operator (FP32 or FP64, as in the forward), and the time step's
+// adjoint routed through the controller (Main_D :162-201): through the patch
+// that set min |V/Accel| / DtCut, through 1.2 x the previous step's Dt, or
+// nowhere (RuptureDt, MaximumDt); retried steps scale it by their halvings.
+namespace {
+
+struct DevMem {
+    std::vector<void*> ptrs;
+    template <class T>
+    int get(T** p, size_t n) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+            return fail(QDFN_ERR_NOMEM, "adjoint buffers");
+        ptrs.push_back(q);
+        *p = reinterpret_cast<T*>(q);
+        return QDFN_OK;
+    }
+    ~DevMem() {
+        for (void* q : ptrs) cudaFree(q);
+    }
+};
+
+// one launch of `nsteps` steps on st, as qdfn_run_async (no status check)
+int launch_steps(qdfn_ctx* c, int64_t nsteps, uint64_t budget_ns, cudaStream_t st) {
+    QDFN_CUDA(cudaMemsetAsync(c->gerr, 0, 2 * sizeof(int), st));
+    SimParams p = make_params(c, budget_ns);
+    SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
+    void* args[] = {&p, &nsteps};
+    QDFN_CUDA(cudaLaunchCooperativeKernel((const void*)k, dim3(c->nblocks), dim3(kSimThreads), args, c->smem, st));
+    return QDFN_OK;
+}
+
+int run_status(qdfn_ctx* c, cudaStream_t st) {
+    QDFN_CUDA(cudaStreamSynchronize(st));
+    int gerr = 0;
+    QDFN_CUDA(cudaMemcpy(&gerr, c->gerr, sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> v(kernel_R(c->R));
+    QDFN_CUDA(cudaMemcpy(v.data(), c->status, v.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int r = 0; r < c->R; ++r)
+        if (v[r] != 0) return fail(v[r], "instance " + std::to_string(r) + " stopped in the adjoint's forward");
+    if (gerr != 0) return fail(gerr, "device loop stopped early in the adjoint's forward");
+    return QDFN_OK;
+}
+
+// the six host-visible state fields (one block), T/dt and step of a context
+struct Snap {
+    double* s6;
+    double* Tdt;
+    int64_t* step;
+};
+int snap_save(qdfn_ctx* c, const Snap& d, cudaStream_t st) {
+    const size_t RN = (size_t)kernel_R(c->R) * c->N, Rk = kernel_R(c->R);
+    QDFN_CUDA(cudaMemcpyAsync(d.s6, c->V, 6 * RN * 8, cudaMemcpyDeviceToDevice, st));
+    QDFN_CUDA(cudaMemcpyAsync(d.Tdt, c->T, 2 * Rk * 8, cudaMemcpyDeviceToDevice, st));
+    QDFN_CUDA(cudaMemcpyAsync(d.step, c->step, Rk * 8, cudaMemcpyDeviceToDevice, st));
+    return QDFN_OK;
+}
+int snap_load(qdfn_ctx* c, const Snap& d, cudaStream_t st) {
+    const size_t RN = (size_t)kernel_R(c->R) * c->N, Rk = kernel_R(c->R);
+    QDFN_CUDA(cudaMemcpyAsync(c->V, d.s6, 6 * RN * 8, cudaMemcpyDeviceToDevice, st));
+    QDFN_CUDA(cudaMemcpyAsync(c->T, d.Tdt, 2 * Rk * 8, cudaMemcpyDeviceToDevice, st));
+    QDFN_CUDA(cudaMemcpyAsync(c->step, d.step, Rk * 8, cudaMemcpyDeviceToDevice, st));
+    return QDFN_OK;
+}
+
+}  // namespace
+
+extern "C" int qdfn_adjoint_run(qdfn_ctx* c, int64_t nsteps, int64_t checkpoint_every, const double* dL_dD_final,
+                                int64_t n_seeds, const int64_t* seed_step, const int32_t* seed_inst,
+                                const int64_t* seed_patch, const double* seed_dV, const double* seed_dD,
+                                const double* seed_dT, double* dL_da, double* dL_db, double* dL_dDc,
+                                double timeout_s) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (c->prec < 0 || c->hmat) return fail(QDFN_ERR_STATE, "the adjoint needs a dense operator (qdfn_set_dense)");
+    if (c->running || (c->ens && ensemble_running(c->ens))) return fail(QDFN_ERR_STATE, "a run is in flight");
+    if (c->prob.alpha_evo != 0.0) return fail(QDFN_ERR_INVALID, "the adjoint supports Alpha_Evo = 0 only");
+    if (nsteps < 1) return fail(QDFN_ERR_INVALID, "nsteps must be >= 1");
+    if (n_seeds < 0 || (n_seeds > 0 && (!seed_step || !seed_inst || !seed_patch || !seed_dV || !seed_dD || !seed_dT)))
+        return fail(QDFN_ERR_INVALID, "seed arrays");
+    if (!dL_da || !dL_db || !dL_dDc) return fail(QDFN_ERR_INVALID, "null gradient output");
+    const int64_t N = c->N, Ns = c->N - c->Nload;
+    const int R = c->R, Rk = kernel_R(c->R);
+    const int64_t RN = (int64_t)Rk * N;
+    for (int64_t k = 0; k < n_seeds; ++k)
+        if (seed_step[k] < 0 || seed_step[k] > nsteps || seed_inst[k] < 0 || seed_inst[k] >= R ||
+            seed_patch[k] < -1 || seed_patch[k] >= N)
+            return fail(QDFN_ERR_INVALID, "seed " + std::to_string(k) + " out of range");
+    int64_t cp = checkpoint_every > 0 ? checkpoint_every : (int64_t)std::ceil(std::sqrt((double)nsteps));
+    cp = std::max<int64_t>(1, std::min(cp, nsteps));
+    const int64_t nseg = (nsteps + cp - 1) / cp;
+    const uint64_t budget_ns = (uint64_t)((timeout_s > 0 ? timeout_s : 1e6) * 1e9);
+    cudaStream_t st = nullptr;
+    int rc;
+    DevMem m;
+    // checkpoints (nseg, the state before each segment) and the final state
+    std::vector<Snap> ck(nseg + 1);
+    for (auto& k : ck)
+        if ((rc = m.get(&k.s6, 6 * RN)) || (rc = m.get(&k.Tdt, 2 * Rk)) || (rc = m.get(&k.step, Rk))) return rc;
+    // tape of one segment: state s = 0..cp (V, D, theta, accel), steps 1..cp (tld, sigma, solver), T and dt
+    double *tV, *tD, *tth, *tA, *ttld, *tsig, *tT, *tdt;
+    unsigned char* tsw;
+    if ((rc = m.get(&tV, (cp + 1) * RN)) || (rc = m.get(&tD, (cp + 1) * RN)) || (rc = m.get(&tth, (cp + 1) * RN)) ||
+        (rc = m.get(&tA, (cp + 1) * RN)) || (rc = m.get(&ttld, cp * RN)) || (rc = m.get(&tsig, cp * RN)) ||
+        (rc = m.get(&tsw, cp * RN)) || (rc = m.get(&tT, (cp + 1) * Rk)) || (rc = m.get(&tdt, (cp + 1) * Rk)))
+        return rc;
+    // adjoint state and work arrays
+    double *lV, *lD, *lth, *lA, *oDloc, *oVold, *oThold, *oTLD, *oSig, *ga, *gb, *gDc, *bdt, *btx, *sums, *part,
+        *ctl, *addv;
+    int64_t* addi;
+    int* derr;
+    const int nblk = adj_local_blocks(RN);
+    const int64_t rpb = c->ld, nrb = (N + rpb - 1) / rpb;
+    const int64_t max_add = std::max<int64_t>(n_seeds + Rk, 1);
+    if ((rc = m.get(&lV, RN)) || (rc = m.get(&lD, RN)) || (rc = m.get(&lth, RN)) || (rc = m.get(&lA, RN)) ||
+        (rc = m.get(&oDloc, RN)) || (rc = m.get(&oVold, RN)) || (rc = m.get(&oThold, RN)) ||
+        (rc = m.get(&oTLD, RN)) || (rc = m.get(&oSig, RN)) || (rc = m.get(&ga, RN)) || (rc = m.get(&gb, RN)) ||
+        (rc = m.get(&gDc, RN)) || (rc = m.get(&bdt, (int64_t)nblk * Rk)) || (rc = m.get(&btx, (int64_t)nblk * Rk)) ||
+        (rc = m.get(&sums, 2 * Rk)) || (rc = m.get(&part, nrb * 2 * RN)) || (rc = m.get(&ctl, 5 * Rk)) ||
+        (rc = m.get(&addv, 3 * max_add)) || (rc = m.get(&addi, max_add)) || (rc = m.get(&derr, 1)))
+        return rc;
+    if ((rc = adj_transpose_prepare(c->prec, Rk, rpb))) return rc;
+    for (double* z : {lV, lD, lth, lA, ga, gb, gDc}) QDFN_CUDA(cudaMemsetAsync(z, 0, RN * 8, st));
+    QDFN_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), st));
+
+    // ---- forward: one step per launch, a checkpoint every cp steps
+    for (int64_t seg = 0; seg < nseg; ++seg) {
+        if ((rc = snap_save(c, ck[seg], st))) return rc;
+        const int64_t len = std::min(cp, nsteps - seg * cp);
+        for (int64_t t = 0; t < len; ++t)
+            if ((rc = launch_steps(c, 1, budget_ns, st))) return rc;
+        if ((rc = run_status(c, st))) return rc;
+    }
+    if ((rc = snap_save(c, ck[nseg], st))) return rc;
+
+    // ---- seeds by step
+    std::vector<std::vector<int64_t>> by_step(nsteps + 1);
+    for (int64_t k = 0; k < n_seeds; ++k) by_step[seed_step[k]].push_back(k);
+    std::vector<double> lamT(Rk, 0.0), carry(Rk, 0.0);
+    if (dL_dD_final) {
+        std::vector<double> h(RN, 0.0);
+        std::memcpy(h.data(), dL_dD_final, (size_t)R * N * 8);
+        QDFN_CUDA(cudaMemcpy(lD, h.data(), RN * 8, cudaMemcpyHostToDevice));
+    }
+    // adds seeds of state n and controller terms to (lV, lD, lA), lamT
+    std::vector<int64_t> hi;
+    std::vector<double> hv;
+    auto apply_adds = [&](const std::vector<int64_t>& idx, const std::vector<double>& vV,
+                          const std::vector<double>& vD, const std::vector<double>& vA) -> int {
+        const int n = (int)idx.size();
+        if (n == 0) return QDFN_OK;
+        std::vector<double> v(3 * (size_t)n);
+        for (int k = 0; k < n; ++k) { v[k] = vV[k]; v[n + k] = vD[k]; v[2 * n + k] = vA[k]; }
+        QDFN_CUDA(cudaMemcpy(addi, idx.data(), n * 8, cudaMemcpyHostToDevice));
+        QDFN_CUDA(cudaMemcpy(addv, v.data(), 3 * (size_t)n * 8, cudaMemcpyHostToDevice));
+        return adj_add(n, addi, addv, lV, lD, lA, st);
+    };
+    auto seeds_of = [&](int64_t n) -> int {
+        std::vector<int64_t> idx;
+        std::vector<double> vV, vD, vA;
+        for (int64_t k : by_step[n]) {
+            lamT[seed_inst[k]] += seed_dT[k];
+            if (seed_patch[k] >= 0) {
+                idx.push_back((int64_t)seed_inst[k] * N + seed_patch[k]);
+                vV.push_back(seed_dV[k]); vD.push_back(seed_dD[k]); vA.push_back(0.0);
+            }
+        }
+        return apply_adds(idx, vV, vD, vA);
+    };
+    if ((rc = seeds_of(nsteps))) return rc;
+
+    const double rupture = c->prob.rupture_dt, maxdt = c->prob.max_dt, swv = c->prob.switch_v, dtcut = c->prob.dt_cut;
+    const bool told = c->prob.interp_at_told != 0;
+    // ---- reverse, segment by segment
+    for (int64_t seg = nseg - 1; seg >= 0; --seg) {
+        const int64_t s0 = seg * cp, len = std::min(cp, nsteps - s0);
+        if ((rc = snap_load(c, ck[seg], st))) return rc;
+        auto rec_state = [&](int64_t t) -> int {   // tape state t from the context's host-visible state
+            QDFN_CUDA(cudaMemcpyAsync(tV + t * RN, c->V, RN * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tD + t * RN, c->D, RN * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tth + t * RN, c->theta, RN * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tA + t * RN, c->accel, RN * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tT + t * Rk, c->T, Rk * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tdt + t * Rk, c->dt, Rk * 8, cudaMemcpyDeviceToDevice, st));
+            return QDFN_OK;
+        };
+        if ((rc = rec_state(0))) return rc;
+        for (int64_t t = 1; t <= len; ++t) {
+            c->sw_used = tsw + (t - 1) * RN;
+            rc = launch_steps(c, 1, budget_ns, st);
+            c->sw_used = nullptr;
+            if (rc) return rc;
+            if ((rc = rec_state(t))) return rc;
+            QDFN_CUDA(cudaMemcpyAsync(ttld + (t - 1) * RN, c->tld, RN * 8, cudaMemcpyDeviceToDevice, st));
+            QDFN_CUDA(cudaMemcpyAsync(tsig + (t - 1) * RN, c->sig_old, RN * 8, cudaMemcpyDeviceToDevice, st));
+        }
+        if ((rc = run_status(c, st))) return rc;
+        std::vector<double> hdt((len + 1) * Rk), hT((len + 1) * Rk);
+        QDFN_CUDA(cudaMemcpy(hdt.data(), tdt, hdt.size() * 8, cudaMemcpyDeviceToHost));
+        QDFN_CUDA(cudaMemcpy(hT.data(), tT, hT.size() * 8, cudaMemcpyDeviceToHost));
+        for (int64_t t = len; t >= 1; --t) {
+            const int64_t n = s0 + t;   // the step taking tape state t-1 to t
+            AdjLocalArgs a{};
+            a.N = N; a.Ns = Ns; a.R = Rk; a.dr = c->prob.evolution_dr; a.interp_at_told = told ? 1 : 0;
+            a.eta = c->eta; a.sigma_min = c->prob.sigma_min;
+            a.Vprev = tV + (t - 1) * RN; a.Dprev = tD + (t - 1) * RN; a.thprev = tth + (t - 1) * RN;
+            a.Vcur = tV + t * RN; a.tld = ttld + (t - 1) * RN; a.sig = tsig + (t - 1) * RN;
+            a.sw = tsw + (t - 1) * RN;
+            a.dt = tdt + t * Rk; a.Tprev = tT + (t - 1) * Rk;
+            a.pa = c->a; a.pb = c->b; a.pDc = c->Dc; a.F0 = c->F0; a.la = c->la; a.lth0 = c->lth0;
+            a.kself = c->kself; a.mass = c->mass; a.omega = c->omega; a.tau0 = c->tau0;
+            a.n_ext = c->n_ext; a.ext_t = c->ext_t; a.ext_n = c->ext_n; a.ext_s = c->ext_s; a.ext_p = c->ext_p;
+            a.lV = lV; a.lD = lD; a.lth = lth; a.lA = lA;
+            a.oDloc = oDloc; a.oVold = oVold; a.oThold = oThold; a.oTLD = oTLD; a.oSig = oSig;
+            a.ga = ga; a.gb = gb; a.gDc = gDc; a.blk_dt = bdt; a.blk_tx = btx; a.sums = sums; a.err = derr;
+            if ((rc = adj_local(a, st))) return rc;
+            AdjTransArgs tr{};
+            tr.N = N; tr.rpb = rpb; tr.nrb = nrb; tr.gx = std::max<int64_t>(1, (4 * num_sms() + nrb - 1) / nrb);
+            tr.E = c->E; tr.Kn = c->Kn; tr.x_s = oTLD; tr.x_n = oSig; tr.part = part;
+            if ((rc = adj_transpose(c->prec, Rk, tr, oDloc, lD, st))) return rc;   // lambda_D of state t-1
+            std::swap(lV, oVold);
+            std::swap(lth, oThold);
+            QDFN_CUDA(cudaMemsetAsync(lA, 0, RN * 8, st));
+            if ((rc = adj_dtctl(Rk, N, Ns, tV + (t - 1) * RN, tA + (t - 1) * RN, c->unstable, c->has_unstable, ctl,
+                                st)))
+                return rc;
+            std::vector<double> hs(2 * Rk), hc(5 * Rk);
+            QDFN_CUDA(cudaMemcpyAsync(hs.data(), sums, hs.size() * 8, cudaMemcpyDeviceToHost, st));
+            QDFN_CUDA(cudaMemcpyAsync(hc.data(), ctl, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+            QDFN_CUDA(cudaStreamSynchronize(st));
+            // the step's dt: its patches, T_n = T_{n-1} + dt, the external-stress
+            // time (TOld + Dt in main, TOld in main_H), the next step's 1.2 Dt
+            std::vector<int64_t> idx;
+            std::vector<double> vV, vD, vA;
+            for (int r = 0; r < Rk; ++r) {
+                const double ldt = hs[r] + lamT[r] + (told ? 0.0 : hs[Rk + r]) + carry[r];
+                lamT[r] += hs[Rk + r];
+                carry[r] = 0.0;
+                // the controller that chose this step's Dt, from state t-1
+                const double dtn = hdt[t * Rk + r], dtp = hdt[(t - 1) * Rk + r];
+                double vmax = hc[r * 5 + 0];
+                if (hc[r * 5 + 1] != 0) vmax = NAN;
+                const double dtmin = hc[r * 5 + 2] / dtcut;
+                const bool usable = hc[r * 5 + 3] != 0;
+                int src = 0;   // 0 constant, 1 min |V/A| / DtCut, 2 1.2 x previous Dt
+                double ref;
+                if (vmax > swv) ref = rupture;
+                else if (dtmin > maxdt) ref = maxdt;
+                else { ref = dtmin; src = usable ? 1 : 0; }
+                double dtc;
+                if (ref <= rupture) dtc = ref;
+                else if (dtp < ref / 1.2) { dtc = dtp * 1.2; src = 2; }
+                else dtc = ref;
+                const double sc = dtn / dtc;
+                const double e2 = std::log2(sc);
+                if (!(sc > 0 && sc <= 1 && std::fabs(e2 - std::round(e2)) < 1e-9)) src = 0;   // e.g. Dt = 1e-3
+                if (src == 1) {
+                    const int64_t k = (int64_t)hc[r * 5 + 4];
+                    double Vk = 0, Ak = 0;
+                    QDFN_CUDA(cudaMemcpy(&Vk, tV + (t - 1) * RN + (int64_t)r * N + k, 8, cudaMemcpyDeviceToHost));
+                    QDFN_CUDA(cudaMemcpy(&Ak, tA + (t - 1) * RN + (int64_t)r * N + k, 8, cudaMemcpyDeviceToHost));
+                    const double q = Vk / Ak, sg = q < 0 ? -1.0 : 1.0;
+                    idx.push_back((int64_t)r * N + k);
+                    vV.push_back(ldt * sc * sg / (Ak * dtcut));
+                    vD.push_back(0.0);
+                    vA.push_back(-ldt * sc * sg * Vk / (Ak * Ak * dtcut));
+                } else if (src == 2) {
+                    carry[r] = 1.2 * sc * ldt;
+                }
+            }
+            if ((rc = apply_adds(idx, vV, vD, vA))) return rc;
+            if ((rc = seeds_of(n - 1))) return rc;
+        }
+    }
+    int herr = 0;
+    QDFN_CUDA(cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return fail(QDFN_ERR_DOMAIN, "a converged solve has a vanishing residual derivative");
+    QDFN_CUDA(cudaMemcpy(dL_da, ga, (size_t)R * N * 8, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(dL_db, gb, (size_t)R * N * 8, cudaMemcpyDeviceToHost));
+    QDFN_CUDA(cudaMemcpy(dL_dDc, gDc, (size_t)R * N * 8, cudaMemcpyDeviceToHost));
+    // the context ends where the forward window ended
+    if ((rc = snap_load(c, ck[nseg], st))) return rc;
+    QDFN_CUDA(cudaStreamSynchronize(st));
+    return QDFN_OK;
+}
+
 
 extern "C" int qdfn_set_blocks(qdfn_ctx* c, int nblocks) {
     if (!c) return fail(QDFN_ERR_INVALID, "null context");
@@ -606,11 +912,14 @@ struct qdfn_ensemble {
     int2* dmap = nullptr;                // device [total]: (member, block within it)
     int* dstat = nullptr;                // device [n] outcome of the last run
     int* hstat = nullptr;                // pinned [n]
+    unsigned* dfill = nullptr;           // device: members that have taken their steps (fill mode)
+    int fill = 0;                        // fill mode on
     cudaStream_t pending = nullptr;
     bool running = false;
     ~qdfn_ensemble() {
         if (hparams) cudaFreeHost(hparams);
         if (hstat) cudaFreeHost(hstat);
+        if (dfill) cudaFree(dfill);
         if (dparams) cudaFree(dparams);
         if (dmap) cudaFree(dmap);
         if (dstat) cudaFree(dstat);
@@ -702,32 +1011,36 @@ int ensemble_check(const qdfn_ensemble* e) {
 extern "C" int qdfn_ensemble_shares(int n, const double* cost, int nsm, int* out) {
     if (n < 1 || !cost || !out) return fail(QDFN_ERR_INVALID, "null or empty argument");
     if (n > nsm) return fail(QDFN_ERR_INVALID, std::to_string(n) + " members need at least as many SMs");
-    double sum = 0;
+    double cmax = 0;
     for (int k = 0; k < n; ++k) {
         if (!(cost[k] > 0) || !std::isfinite(cost[k])) return fail(QDFN_ERR_INVALID, "costs must be positive");
-        sum += cost[k];
+        cmax = std::max(cmax, cost[k]);
     }
-    // at least one block each, then the rest by largest remainder of the ideal
-    // (proportional) split; ties to the lower index
-    std::vector<double> ideal(n);
+    // Member k on b blocks takes cost[k] / b.  The smallest makespan T whose
+    // shares ceil(cost[k] / T) fit in nsm blocks (bisection on T), then the
+    // blocks left over one by one to the member with the longest time.
+    auto need = [&](double T) {
+        long long s = 0;
+        for (int k = 0; k < n; ++k) s += (long long)std::max(1.0, std::ceil(cost[k] / T * (1 - 1e-12)));
+        return s;
+    };
+    double lo = cmax / nsm, hi = cmax;   // need(hi) = n <= nsm
+    for (int it = 0; it < 200 && hi - lo > 1e-12 * hi; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (need(mid) <= nsm) hi = mid; else lo = mid;
+    }
     int used = 0;
     for (int k = 0; k < n; ++k) {
-        ideal[k] = nsm * cost[k] / sum;
-        out[k] = std::max(1, (int)std::floor(ideal[k]));
+        out[k] = (int)std::max(1.0, std::ceil(cost[k] / hi * (1 - 1e-12)));
         used += out[k];
     }
-    while (used > nsm) {   // the floors of 1 pushed the sum over: trim the largest
-        int big = 0;
+    while (used < nsm) {
+        int worst = 0;
         for (int k = 1; k < n; ++k)
-            if (out[k] > out[big]) big = k;
-        --out[big];
-        --used;
+            if (cost[k] / out[k] > cost[worst] / out[worst]) worst = k;
+        ++out[worst];
+        ++used;
     }
-    std::vector<int> order(n);
-    for (int k = 0; k < n; ++k) order[k] = k;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return ideal[a] - out[a] > ideal[b] - out[b]; });
-    for (int k = 0; k < n && used < nsm; ++k, ++used) ++out[order[k]];
     return QDFN_OK;
 }
 
@@ -763,7 +1076,8 @@ extern "C" int qdfn_ensemble_create(qdfn_ensemble** out, int n, qdfn_ctx* const*
     if (!rc && (cudaMallocHost(&e->hparams, sizeof(SimParams) * n) != cudaSuccess ||
                 cudaMallocHost(&e->hstat, sizeof(int) * n) != cudaSuccess ||
                 cudaMalloc(&e->dparams, sizeof(SimParams) * n) != cudaSuccess ||
-                cudaMalloc(&e->dstat, sizeof(int) * n) != cudaSuccess))
+                cudaMalloc(&e->dstat, sizeof(int) * n) != cudaSuccess ||
+                cudaMalloc(&e->dfill, sizeof(unsigned)) != cudaSuccess))
         rc = fail(QDFN_ERR_NOMEM, "ensemble buffers");
     if (!rc) rc = ensemble_configure(e);
     if (rc) {
@@ -877,9 +1191,15 @@ extern "C" int qdfn_ensemble_run_async(qdfn_ensemble* e, int64_t nsteps, double 
     const uint64_t budget_ns = (uint64_t)(budget * 1e9);
     cudaStream_t st = (cudaStream_t)stream;
     const int n = (int)e->m.size();
-    for (int k = 0; k < n; ++k) e->hparams[k] = make_params(e->m[k], budget_ns);
+    for (int k = 0; k < n; ++k) {
+        e->hparams[k] = make_params(e->m[k], budget_ns);
+        if (e->fill) {
+            e->hparams[k].fill_ctr = e->dfill;
+            e->hparams[k].fill_need = (unsigned)n;
+        }
+    }
     QDFN_CUDA(cudaMemcpyAsync(e->dparams, e->hparams, sizeof(SimParams) * n, cudaMemcpyHostToDevice, st));
-    if ((rc = members_reset(e->dparams, n, st))) return rc;
+    if ((rc = members_reset(e->dparams, n, e->dfill, st))) return rc;
     const MembersKernel k = members_kernel(e->prec, e->Rk);
     const SimParams* dp = e->dparams;
     const int2* dm = e->dmap;
@@ -899,6 +1219,13 @@ extern "C" int qdfn_ensemble_sync(qdfn_ensemble* e) {
     QDFN_CUDA(cudaStreamSynchronize(e->pending));
     for (size_t k = 0; k < e->m.size(); ++k)
         if (e->hstat[k] != 0) return fail(e->hstat[k], "ensemble member " + std::to_string(k) + " stopped");
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_ensemble_set_fill(qdfn_ensemble* e, int on) {
+    if (!e) return fail(QDFN_ERR_INVALID, "null ensemble");
+    if (e->running) return fail(QDFN_ERR_STATE, "a run is in flight");
+    e->fill = on ? 1 : 0;
     return QDFN_OK;
 }
 

@@ -129,6 +129,14 @@ struct SimParams {
     int rb_ordered;                  // FP32/BF16 dense: row blocks with high-velocity patches first
     int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
     int spec_stop;                   // no early-tile claims once this many blocks reached the step's barrier
+    // ensemble "fill" mode (null: off): a member that has taken its nsteps
+    // steps adds one to *fill_ctr and keeps stepping until fill_need members
+    // have, so that no SM idles while the slowest member finishes
+    unsigned* fill_ctr;
+    unsigned fill_need;
+    // adjoint recording (null: off): the solver each patch's accepted pass
+    // used, [R][N] (0 low velocity, 1 high velocity, 2 loading fault)
+    unsigned char* sw_used;
     unsigned long long* tmax;        // [kSets][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, last row block complete), ns
 };
@@ -990,6 +998,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
     __shared__ double s_rdt[kMaxInst];   // 1/s_dt, correctly rounded, formed before each solve pass
     __shared__ int64_t s_step[kMaxInst], s_nrec[kMaxInst];
     __shared__ int s_done[kMaxInst], s_fail[kMaxInst], s_stop, s_par;
+    __shared__ int s_fill_stop, s_fill_counted;   // fill mode: every member has its nsteps; this one counted
     __shared__ int s_iter;
     // this block's reduction of a solve pass, as order-preserving keys (exact
     // min/max, integer pipe), one set per instance: [0] min flag, [1] min Dt,
@@ -1023,7 +1032,13 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
         s_nrec[threadIdx.x] = p.nrec[threadIdx.x];
         s_fail[threadIdx.x] = p.status[threadIdx.x];
     }
-    if (threadIdx.x == 0) { s_stop = 0; s_par = 0; }
+    if (threadIdx.x == 0) { s_stop = 0; s_par = 0; s_fill_stop = 0; s_fill_counted = 0; }
+    // fill mode: whether every member has taken its nsteps (read into each
+    // block's reduction slot, so that the member's blocks decide together)
+    auto fill_seen = [&](int64_t it) -> double {
+        if (p.fill_ctr == nullptr || it + 1 < nsteps) return 0.0;
+        return *(volatile unsigned*)p.fill_ctr >= p.fill_need ? 1.0 : 0.0;
+    };
     auto red_slot = [&](int ph, int64_t blk, int r) -> double* {
         return p.red + (((int64_t)(ph & 1) * p.nblk + blk) * R + r) * kRedSlots;
     };
@@ -1067,6 +1082,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 double* s = red_slot(phase, blk, r);
                 s[4] = v[r][0]; s[5] = v[r][1]; s[6] = v[r][2]; s[7] = v[r][3];
                 s[8] = (globaltimer_ns() > deadline) ? 1.0 : 0.0;
+                s[9] = 0.0;
             }
             if (blk == 0 && HM) atomicExch(p.tile_ctr, 0ull);
         }
@@ -1093,11 +1109,18 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
     }
     lap(0);
 
-    for (int64_t it = 0; it < nsteps; ++it) {
+    for (int64_t it = 0; it < nsteps || p.fill_ctr != nullptr; ++it) {
         {
             int stop = s_stop;
             for (int r = 0; r < R; ++r) stop |= (s_fail[r] != 0);
             if (stop) break;
+        }
+        if (it >= nsteps) {   // fill mode: this member has its steps
+            if (blk == 0 && threadIdx.x == 0 && !s_fill_counted) {
+                s_fill_counted = 1;
+                atomicAdd(p.fill_ctr, 1u);
+            }
+            if (s_fill_stop) break;
         }
         const int par = s_par;             // which buffer holds the current state
         const int cpar = (int)(it % kSets);   // which counter set this step uses
@@ -1123,7 +1146,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
         // belongs to another launch)
         StepCtx sc{cpar, cnext, (int)(it & 1), xdc,
                    reinterpret_cast<const X*>(p.xd) + (size_t)(par ^ 1) * p.xd_stride, 0,
-                   (!HM && sizeof(X) == 4 && p.c_spec > 0 && it + 1 < nsteps) ? 1 : 0};
+                   (!HM && sizeof(X) == 4 && p.c_spec > 0 && (it + 1 < nsteps || p.fill_ctr != nullptr)) ? 1 : 0};
         sc.order = use_order ? s_order[it & 1] : nullptr;
         if (pre) sc.spec_done = s_next_spec_done;
         // one (instance r, patch i) item of a solve pass; pass 0 of a step also
@@ -1190,6 +1213,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                     o = sim::solve_lowv(pin, Dt, p.eta, p.alpha_evo, p.evolution_dr, p.switch_v, err);
                 }
                 if (!writer) return;
+                if (p.sw_used) p.sw_used[q] = (unsigned char)swq;
                 QDFN_NXT(V, Vn)[q] = o.V; QDFN_NXT(fric, fn)[q] = o.Friction; QDFN_NXT(D, Dn)[q] = o.Disp;
                 QDFN_NXT(theta, thn)[q] = o.Theta; QDFN_NXT(sig_old, sn)[q] = sig;
                 p.dtall[q] = o.Dt; p.instab[q] = o.Instab; p.flag[q] = o.Flag;
@@ -1207,6 +1231,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 if constexpr (!HM) reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)o.Disp;
             } else {
                 if (!writer) return;   // loading faults (Solvers :370-377)
+                if (p.sw_used) p.sw_used[q] = 2;
                 const double Vc = p.Vconst[q];
                 const double Dn = QDFN_CUR(D, Dn)[q] + Vc * Dt;
                 QDFN_NXT(V, Vn)[q] = Vc; QDFN_NXT(fric, fn)[q] = QDFN_CUR(fric, fn)[q]; QDFN_NXT(D, Dn)[q] = Dn;
@@ -1402,6 +1427,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                         double* sl = red_slot(phase, blk, r);
                         for (int k = 0; k < 8; ++k) sl[k] = ord_val(s_red[r][k]);
                         sl[8] = late;
+                        sl[9] = fill_seen(it);
                     }
                 }
                 const uint64_t t_items = gt == 0 ? globaltimer_ns() : 0;
@@ -1437,13 +1463,14 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                         }
                     }
                     if (r < R) {
-                        const int ops[9] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
-                        double f[9];
-                        grid_fields<9>(p.red + (int64_t)(phase & 1) * p.nblk * R * kRedSlots, p.nblk, R, r,
-                                       ops, f);
+                        const int ops[10] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0};
+                        double f[10];
+                        grid_fields<10>(p.red + (int64_t)(phase & 1) * p.nblk * R * kRedSlots, p.nblk, R, r,
+                                        ops, f);
                         const double mflag = f[0], mdt = f[1], any4 = f[2], err = f[3];
                         if ((threadIdx.x & 31) == 0) {
                             if (f[8] != 0) s_stop = 1;
+                            if (f[9] != 0) s_fill_stop = 1;
                             if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
                             else if (mflag == 0) {
                                 s_dt[r] = any4 != 0 ? 1e-3 : mdt;
@@ -1522,6 +1549,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                     double* s = red_slot(phase, blk, r);
                     for (int k = 0; k < 8; ++k) s[k] = ord_val(s_red[r][k]);
                     s[8] = late;
+                    s[9] = fill_seen(it);
                 }
             }
             const uint64_t t_items = threadIdx.x == 0 ? globaltimer_ns() : 0;
@@ -1548,13 +1576,14 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             if ((threadIdx.x >> 5) < R) {
                 const int r = threadIdx.x >> 5;
                 if (!s_done[r]) {
-                    const int ops[9] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
-                    double f[9];
-                    grid_fields<9>(p.red + (int64_t)(phase & 1) * p.nblk * R * kRedSlots, p.nblk, R, r, ops,
-                                   f);
+                    const int ops[10] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0};
+                    double f[10];
+                    grid_fields<10>(p.red + (int64_t)(phase & 1) * p.nblk * R * kRedSlots, p.nblk, R, r, ops,
+                                    f);
                     const double mflag = f[0], mdt = f[1], any4 = f[2], err = f[3];
                     if ((threadIdx.x & 31) == 0) {
                         if (f[8] != 0) s_stop = 1;   // benign race: every writer stores 1
+                        if (f[9] != 0) s_fill_stop = 1;
                         if (err != 0) { s_fail[r] = (int)err; s_done[r] = 1; }
                         else if (mflag == 0) {
                             s_dt[r] = any4 != 0 ? 1e-3 : mdt;
@@ -1629,6 +1658,9 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
         lap(3);
         n_steps++;
     }
+    // fill mode: a member that ended before its nsteps (a failure) still counts,
+    // so that the others stop
+    if (p.fill_ctr != nullptr && blk == 0 && threadIdx.x == 0 && !s_fill_counted) atomicAdd(p.fill_ctr, 1u);
     // the state back into the host-visible buffers when it ended in the others
     if (s_par) {
         const StateView a = state_view(p, 0), b = state_view(p, 1);

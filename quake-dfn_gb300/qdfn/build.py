@@ -31,6 +31,7 @@ UNITS = {
     "ensemble.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "selfcheck.cu": ["--fmad=false"],
+    "adjoint.cu": ["--fmad=false"],
 }
 
 

@@ -19,8 +19,8 @@ from . import _lib, simulate
 
 
 def sm_shares(cost, n_sms):
-    """Blocks per member: at least one each, in proportion to ``cost``, summing
-    to at most ``n_sms`` (largest remainder) -- the library's split rule
+    """Blocks per member: at least one each, minimising the longest member
+    time cost/blocks, summing to ``n_sms`` -- the library's split rule
     (qdfn_ensemble_shares, host code, no GPU needed)."""
     cost = np.ascontiguousarray(np.asarray(cost, dtype=np.float64))
     out = np.zeros(cost.shape[0], dtype=np.int32)
@@ -92,6 +92,15 @@ class Ensemble:
             self.balance()
             hist.append(self.blocks.copy())
         return hist
+
+    def set_fill(self, on=True):
+        """Fill mode: members that have taken the run's nsteps keep stepping
+        until every member has, so that no SM idles (qdfn_ensemble_set_fill)."""
+        _lib.check(self.L.qdfn_ensemble_set_fill(self._h, 1 if on else 0))
+
+    def steps(self):
+        """Step count of every instance of every member."""
+        return np.asarray([sim.state(r)["step"] for sim in self.members for r in range(sim.n_inst)])
 
     def run_async(self, nsteps, timeout_s=0.0, stream=None):
         _lib.check(self.L.qdfn_ensemble_run_async(self._h, int(nsteps), float(timeout_s),

@@ -16,8 +16,10 @@ def test_sm_shares_are_proportional_and_fit():
     assert s.sum() == 152 and list(s) == [19, 19, 38, 76]
     s = sm_shares([1e6] + [1.0] * 20, 152)          # tiny members still get one SM each
     assert s.sum() == 152 and s.min() == 1 and s[0] == 152 - 20
-    s = sm_shares([3.0, 1.0, 1.0], 4)                # largest remainder: 2.4 / 0.8 / 0.8 -> 2, 1, 1
+    s = sm_shares([3.0, 1.0, 1.0], 4)                # longest time 1.5 (3/2), the others 1
     assert list(s) == [2, 1, 1]
+    s = sm_shares([5.0, 2.0, 2.0, 1.0], 7)           # the smallest longest time on 7 blocks is 2.0
+    assert s.sum() == 7 and max(c / b for c, b in zip([5.0, 2.0, 2.0, 1.0], s)) == 2.0
     with pytest.raises(_lib.QdfnError):
         sm_shares(np.ones(200), 152)                 # more members than SMs
     with pytest.raises(_lib.QdfnError):
