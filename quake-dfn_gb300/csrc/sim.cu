@@ -222,7 +222,7 @@ int configure_launch(qdfn_ctx* c) {
         c->smem = (size_t)Rk * hmat::kChunk * xsz + (size_t)hmat::kMaxRank * Rk * sizeof(double);
         c->nchunk = c->nchunk2 = 0;
         c->chunk_len = c->chunk_len2 = c->rb_small0 = 0;
-        want_blocks = std::max<int64_t>(c->hops.n_tiles, c->hops.n_lr);
+        want_blocks = (std::max<int64_t>(c->hops.n_tiles, c->hops.n_lr) + kSimThreads / 32 - 1) / (kSimThreads / 32);
     } else {
         // column chunks of at most 2048 sources staged in shared memory per instance,
         // enough (row block, chunk) tiles for >= 2 per SM
@@ -1484,7 +1484,7 @@ extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, c
                 return fail(QDFN_ERR_INVALID, "block range out of [0, N)");
             hmat::Blk& B = blk[side * nb + b];
             B.s0 = s0; B.ns = s1 - s0 + 1; B.r0 = r0; B.nr = r1 - r0 + 1;
-            if (B.nr > ((int64_t)1 << 20) * hmat::kTileRows) return fail(QDFN_ERR_INVALID, "block too tall");
+            if (B.nr > ((int64_t)1 << 20) * hmat::kSliceRows) return fail(QDFN_ERR_INVALID, "block too tall");
             B.slot = slot;
             slot += B.nr;
             if (rank[b] < 0) {
@@ -1563,12 +1563,27 @@ extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, c
         // normal rows index rowslot from base_n: shift the normal CSR
         for (int64_t i = 0; i <= N; ++i) rowptr[(N + 1) + i] += base_n;
     }
-    std::vector<int64_t> lr, tiles;
+    // warp tasks, largest first: pass A one per (low-rank block, rank row)
+    // (cost ns), pass B one per (block, 64-row slice) (cost rows x inner size;
+    // a rank-0 block's task writes zero partials)
+    std::vector<std::pair<int64_t, int64_t>> ta, tb;   // (cost, code)
     for (int64_t q = 0; q < 2 * nb; ++q) {
-        if (blk[q].rank >= 0 && blk[q].rank > 0) lr.push_back(q);
-        const int64_t nt = (blk[q].nr + hmat::kTileRows - 1) / hmat::kTileRows;
-        for (int64_t t = 0; t < nt; ++t) tiles.push_back((q << 20) | t);
+        const hmat::Blk& B = blk[q];
+        if (B.rank > 0)
+            for (int64_t kk = 0; kk < B.rank; ++kk) ta.push_back({B.ns, (q << 8) | kk});
+        const int64_t inner = B.rank < 0 ? B.ns : B.rank;
+        const int64_t nt = (B.nr + hmat::kSliceRows - 1) / hmat::kSliceRows;
+        for (int64_t t = 0; t < nt; ++t)
+            tb.push_back({std::min<int64_t>(hmat::kSliceRows, B.nr - t * hmat::kSliceRows) * inner, (q << 20) | t});
     }
+    auto by_cost = [](const std::pair<int64_t, int64_t>& x, const std::pair<int64_t, int64_t>& y) {
+        return x.first != y.first ? x.first > y.first : x.second < y.second;
+    };
+    std::sort(ta.begin(), ta.end(), by_cost);
+    std::sort(tb.begin(), tb.end(), by_cost);
+    std::vector<int64_t> lr, tiles;
+    for (auto& x : ta) lr.push_back(x.second);
+    for (auto& x : tb) tiles.push_back(x.second);
     // device copies
     release_hmat(c);
     c->release(c->E); c->release(c->Kn);

@@ -51,12 +51,16 @@ __device__ __forceinline__ bool alpha_term_zero(double alpha, double Dt, double 
 }
 
 // Division by a divisor that stays fixed for a whole solve.  With y = 1/d
-// correctly rounded (one IEEE division per solve), q0 = x*y is within an ulp
-// of x/d, the remainder r = x - q0*d is exact in one FMA, and q0 + r*y rounds
-// to x/d (Markstein's correction step: P. Markstein, "Computation of elementary
-// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
-// 1990).  Three FP64 operations instead of the eight of a full division.  The
-// sum is formed as -fma(-r, y, -q0) so that x = -0 keeps its sign.  Operands
+// correctly rounded (one IEEE division per solve), q0 = x*y is within two ulps
+// of x/d, the remainder r = x - q0*d is exact in one FMA, and q0 + r*y is x/d
+// up to an error of about 2^-52 ulp before its rounding (Markstein's correction
+// step: P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990), so it rounds to the
+// IEEE quotient unless x/d lies that close to a rounding boundary; the GPU
+// test of this helper checks it bit for bit against IEEE division on random
+// operands and on hard cases.  Three FP64 operations instead of the eight of a
+// full division.  A
+// zero dividend returns q0 = x * y, whose sign is IEEE's for x / d.  Operands
 // whose magnitudes leave [2^-895, 2^896] (or a divisor that is zero, infinite
 // or NaN) take the full division, so no step can overflow or underflow.
 struct Recip {
@@ -87,7 +91,7 @@ __device__ __forceinline__ double div_by(double x, const Recip& R) {
     const double q = -fma(-r, R.y, -q0);
     const bool zero = (__double_as_longlong(x) << 1) == 0;
     const bool fast = R.ok && (zero || (in_safe_range(exp_field(x)) && in_safe_range(exp_field(q0))));
-    if (fast) return q;
+    if (fast) return zero ? q0 : q;   // a zero dividend: q0 = x * (1/d) carries the IEEE sign
     return full_div(x, R.d);   // out of line: never evaluated speculatively
 }
 

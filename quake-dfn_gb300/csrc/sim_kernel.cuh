@@ -262,7 +262,6 @@ __device__ __forceinline__ void grid_fields(const double* slots_base, int nblk, 
 // persistent kernel.  x = D (all R instances) is staged per tile.  FP32/BF16
 // products are summed in FP32 over 32 columns and folded error-free into
 // (hi, lo) FP32 pairs; FP64 storage accumulates in FP64.
-static_assert(hmat::kTileRows == kSimThreads, "H-matrix row tiles are one row per thread");
 constexpr int kOpWarps = 8;                                     // operator role: warps [0, kOpWarps)
 constexpr int kOpThreads = kOpWarps * 32;
 constexpr int kProducerWarp = kSimThreads / 32 - 1;             // lane 0 fills the stage ring

@@ -21,6 +21,9 @@ import numpy as np
 from . import _lib
 
 
+MAX_RANK = 128   # the device's rank limit of a low-rank block (larger: stored dense)
+
+
 class ClusterTree:
     """Binary tree over patch centres; `perm` orders patches so every node is a
     contiguous index range [start, end)."""
@@ -263,8 +266,8 @@ def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf
         for side, (Ul, Vl, Dl) in enumerate(((us, vs, ds), (un, vn, dn))):
             row = lambda i: block(s0, s1, r0 + i, r0 + i + 1)[side][0].clone()
             col = lambda j: block(s0 + j, s0 + j + 1, r0, r1)[side][:, 0].clone()
-            U, Vt = aca_fn(row, col, nr, ns, tol, device=device, dtype=torch.float64)
-            if U.shape[1] * (nr + ns) < nr * ns:
+            U, Vt = aca_fn(row, col, nr, ns, tol, max_rank=MAX_RANK, device=device, dtype=torch.float64)
+            if U.shape[1] < MAX_RANK and U.shape[1] * (nr + ns) < nr * ns:
                 Ul.append(U.cpu().numpy()); Vl.append(Vt.cpu().numpy()); Dl.append(None)
             else:
                 B = block(s0, s1, r0, r1)[side]
