@@ -59,12 +59,15 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="ensemble", choices=["network", "ensemble"],
+    ap.add_argument("--workload", default="ensemble", choices=["network", "ensemble", "tri_h"],
                     help="ensemble (default, C4): 64 fault networks of 800-6,000 patches x 4 friction draws in "
                          "one persistent launch; network (C2): the 30-fault network x 4 draws")
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--cpu-members", type=int, default=4,
                     help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
+    ap.add_argument("--rebalance-every", type=int, default=250,
+                    help="ensemble: steps per launch in the timed window, the SMs re-divided between launches "
+                         "(0: one launch)")
     ap.add_argument("--no-fill", dest="fill", action="store_false",
                     help="skip the fill-mode measurement of the ensemble window")
     ap.add_argument("--horizon", type=int, default=1000,
@@ -696,7 +699,7 @@ def run_ensemble(args):
 
     # ---- accuracy horizon: mixed vs FP64 from t = 0, every 100 steps.  A
     # member counts as interseismic until its FP64 run first has a patch past
-    # ten times the starting slip rate (at a check) or on the high-velocity
+    # twice the starting slip rate (at a check) or on the high-velocity
     # solver; a nucleation's runaway amplifies any perturbation (a 1e-15
     # perturbation of the FP64 operator alone grows to ~1e-7 through an
     # event), so the 1e-6 contract is stated over each member's interseismic
@@ -716,7 +719,7 @@ def run_ensemble(args):
             e = _ens_slip_err(ens, ens64).reshape(len(ens.members), R)
             hi = [sim.counters()["highv_solves"] for sim in ens64.members]
             pre &= np.array([h == h0 for h, h0 in zip(hi, hi0)])
-            pre &= np.array([max(float(np.max(sim.state(r)["V"])) for r in range(sim.n_inst)) <= 10 * v0[m]
+            pre &= np.array([max(float(np.max(sim.state(r)["V"])) for r in range(sim.n_inst)) <= 2 * v0[m]
                              for m, sim in enumerate(ens64.members)])
             ep = e[pre]
             errs.append((done, float(e.max()), float(np.median(e)), int(pre.sum() * R),
@@ -746,14 +749,31 @@ def run_ensemble(args):
     clocks.start()
     time.sleep(0.3)
     cnt0 = [sim.counters() for sim in ens.members]
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    ens.run_async(args.steps, timeout_s=TIMEOUT, stream=stream.cuda_stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ens.sync()
+
+    def chunked(e):
+        """K steps as launches of `rebalance_every` steps with the autotuner's
+        re-division of the SMs between them (a member that enters an event
+        gets more SMs for its slow steps); CUDA events bracket all of it, host
+        gaps included.  Returns (ms, launches)."""
+        per = args.rebalance_every if args.rebalance_every > 0 else args.steps
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        done, nl = 0, 0
+        while done < args.steps:
+            n = min(per, args.steps - done)
+            e.run_async(n, timeout_s=TIMEOUT, stream=stream.cuda_stream)
+            nl += 1
+            done += n
+            if done < args.steps:
+                e.sync()
+                e.balance()
+        g1.record(stream)
+        torch.cuda.synchronize()
+        e.sync()
+        return g0.elapsed_time(g1), nl
+
+    ms, nlaunch = chunked(ens)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
     if ws > 1:
         ms = max_over_ranks(ms, dev)
         torch.distributed.barrier()
@@ -812,13 +832,7 @@ def run_ensemble(args):
         start64 = _snapshot(ens64)
         z0 = ens64.sim_years()
         torch.cuda.synchronize()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        ens64.run_async(args.steps, timeout_s=TIMEOUT, stream=stream.cuda_stream)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        ens64.sync()
-        ms64 = f0.elapsed_time(f1)
+        ms64, _ = chunked(ens64)
         yrs64 = float(np.sum(ens64.sim_years() - z0))
         fill64 = fill_window(ens64, start64) if args.fill else None
         # the FP64 operator products are FP64-FMA bound: 2 matrices x R draws
@@ -895,9 +909,10 @@ def run_ensemble(args):
                        "precision": args.precision, "parallelism": "replicas",
                        "l2": "operator %.2f GB per ensemble step > 129 MB L2 (no flush needed)" % (mat_bytes / 1e9),
                        "sm_shares_initial": shares0, "sm_shares_tuned": [int(b) for b in ens.blocks],
+                       "launches": nlaunch, "rebalance_every": args.rebalance_every,
                        "steps_per_instance": [int(min(steps_done)), int(max(steps_done))],
                        "sim_years_in_window": yrs_all},
-            "gpu_launches": 3,
+            "gpu_launches": 3 * nlaunch,
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -979,12 +994,102 @@ def run_reference_ensemble(args):
     print(json.dumps(line))
 
 
+def run_tri_h(args):
+    """C3: 5 curved faults meshed into ~50,000 triangles (TDstressHS), H-matrix
+    operator (cluster-tree leaf 64, admissibility eta = 2, ACA 1e-6), low-rank
+    and near-field blocks stored in FP32 (or --precision fp64), one instance,
+    main_H semantics.  value = simulated years per hour over K steps of one
+    persistent launch; roofline = the stored block bytes streamed per step."""
+    import torch
+    from qdfn import geometry, hmatrix, simulate, synth
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    net = synth.curved_fault_network(seed=args.seed)
+    seg = net["seg"]
+    P1, P2, P3, un, _, _, us = geometry.rot_verts_unit_vectors_abi(seg, seg[:, 9])
+    cen = (P1 + P2 + P3) / 3
+    t0 = time.perf_counter()
+    H, perm = hmatrix.build_tri(P1, P2, P3, seg[:, 9], cen, un, us, net["G"], net["nu"], leaf=64, eta=2.0, tol=1e-6)
+    build_s = time.perf_counter() - t0
+    N = net["N"]
+    kdiag = np.zeros(N)
+    for b, (s0, s1, r0, r1) in enumerate(H.ranges):
+        if s0 == r0 and s1 == r1 and H.dense_s[b] is not None:
+            kdiag[r0:r1 + 1] = np.diag(H.dense_s[b])
+    sysd = {k: (v[perm] if isinstance(v, np.ndarray) and v.shape == (N,) else v) for k, v in net.items()}
+    prob = synth.problem_dict(sysd, kdiag)
+    prob["interp_at_told"] = 1
+    ext = synth.external_ramp(N, net["stressing_rate"], 1e12)
+    esz = {"fp32": 4, "bf16x2": 4, "fp64": 8}[args.precision]
+    stored = H.stored_entries()
+    prec = "fp64" if args.precision == "fp64" else "fp32"
+
+    def make(prec):
+        sim = simulate.Simulation(prob)
+        hmatrix.set_hmatrix(sim, H, prec)
+        sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+        return sim
+
+    def timed(sim):
+        sim.run(args.warmup, timeout_s=TIMEOUT)
+        T0 = sim.state(0)["T"]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run_async(args.steps, stream=stream.cuda_stream, timeout_s=TIMEOUT)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sim.sync()
+        ms = e0.elapsed_time(e1)
+        return ms, (sim.state(0)["T"] - T0) / YEAR
+
+    sim = make(prec)
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    ms, yrs = timed(sim)
+    clk = clocks.stop()
+    sim.close()
+    fp64 = None
+    if not args.no_fp64 and prec != "fp64":
+        s64 = make("fp64")
+        ms64, yrs64 = timed(s64)
+        s64.close()
+        fp64 = {"value": yrs64 / (ms64 / 1e3 / 3600.0), "ms_per_step": ms64 / args.steps,
+                "mixed_over_fp64": (yrs / ms) / (yrs64 / ms64)}
+    peak, peak_kind = measured_peaks()
+    alg = args.steps * stored * esz
+    achieved = alg / (ms / 1e3) / 1e9
+    nlr = sum(1 for U in H.U_s + H.U_n if U is not None)
+    ranks = [U.shape[1] for U in H.U_s + H.U_n if U is not None]
+    line = {"metric": "sim-years/hour, triangle-mesh network with H-matrix operator", "value": yrs / (ms / 1e3 / 3600.0),
+            "unit": "sim-years/hour", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "%s-operator/fp64-state" % prec, "data": "synthetic (seeded curved fault meshes)",
+            "config": {"workload": "C3: 5 curved faults, %d triangles (TDstressHS), H-matrix leaf 64, eta 2, ACA 1e-6, "
+                                   "blocks %s" % (N, prec),
+                       "patches": N, "blocks": int(H.nblocks), "low_rank_blocks": nlr,
+                       "max_rank": int(max(ranks)) if ranks else 0, "mean_rank": float(np.mean(ranks)) if ranks else 0,
+                       "stored_entries": int(stored), "compression_vs_dense": float(stored / (2.0 * N * N)),
+                       "h_build_s": build_s},
+            "gpu_launches": 1,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None,
+                         "note": "k_sim<H> persistent kernel, algorithmic bytes = K x stored block bytes "
+                                 "(%d entries x %d B); peak %s" % (stored, esz, peak_kind)},
+            "fp64_gpu": fp64, "clocks": clk}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference_ensemble(args) if args.workload == "ensemble" else run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
+    elif args.workload == "tri_h":
+        run_tri_h(args)
     else:
         run_ours(args)
 

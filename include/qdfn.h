@@ -95,6 +95,18 @@ int qdfn_assemble_tri_dev(int64_t n_src, const double* P1, const double* P2, con
                           double poisson, double* Ks, double* Kn, int64_t ld, int layout,
                           void* stream);
 
+/* Gathered entries of the triangle stiffness (device pointers): for pair k,
+ * Ks[k], Kn[k] = the (receiver recv_idx[k], source src_idx[k]) entries of
+ * StiffnessMatrix_ByParts_Calculation_Tri (Functions_BuildInputFile.jl:551-594),
+ * indices into the same per-triangle arrays as qdfn_assemble_tri_dev.  The
+ * rows and columns that adaptive cross approximation of an H-matrix block asks
+ * for (the role of HmatBuild_T's block assembly, :643-723), formed without
+ * assembling the block. */
+int qdfn_assemble_tri_pairs_dev(int64_t npairs, const int64_t* recv_idx, const int64_t* src_idx,
+                                const double* P1, const double* P2, const double* P3, const double* rake,
+                                const double* centre, const double* nhat, const double* shat,
+                                double shear_modulus, double poisson, double* Ks, double* Kn, void* stream);
+
 /* ---- cycle simulation ------------------------------------------------------ */
 typedef struct qdfn_ctx qdfn_ctx;
 

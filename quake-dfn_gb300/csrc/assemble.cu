@@ -100,6 +100,22 @@ extern "C" int qdfn_assemble_tri_dev(int64_t n_src, const double* P1, const doub
     return QDFN_OK;
 }
 
+extern "C" int qdfn_assemble_tri_pairs_dev(int64_t npairs, const int64_t* recv_idx, const int64_t* src_idx,
+                                           const double* P1, const double* P2, const double* P3,
+                                           const double* rake, const double* centre, const double* nhat,
+                                           const double* shat, double G, double nu, double* Ks, double* Kn,
+                                           void* stream) {
+    if (npairs < 0) return fail(QDFN_ERR_INVALID, "npairs < 0");
+    if (npairs == 0) return QDFN_OK;
+    if ((npairs + kAsmThreads - 1) / kAsmThreads > 2147483647LL) return fail(QDFN_ERR_INVALID, "too many pairs");
+    if (!recv_idx || !src_idx || !P1 || !P2 || !P3 || !rake || !centre || !nhat || !shat || !Ks || !Kn)
+        return fail(QDFN_ERR_INVALID, "null pointer");
+    launch_assemble_tri_pairs((cudaStream_t)stream, npairs, recv_idx, src_idx, P1, P2, P3, rake, centre, nhat, shat,
+                              G, nu, Ks, Kn);
+    QDFN_CUDA(cudaGetLastError());
+    return QDFN_OK;
+}
+
 extern "C" int qdfn_assemble_tri(int64_t n_src, const double* P1, const double* P2,
                                  const double* P3, const double* rake, int64_t n_recv,
                                  const double* centre, const double* nhat, const double* shat,

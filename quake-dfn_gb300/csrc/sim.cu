@@ -55,6 +55,7 @@ struct qdfn_ctx {
     int *instab, *flag, *sw, *sw_n;
     double* accel_n;
     double *part_s = nullptr, *part_n = nullptr;
+    size_t part_cap = 0, partn_cap = 0, red_cap = 0, xd_cap = 0;   // elements held by the work buffers
     double *T, *dt;
     int64_t *step, *nrec;
     int* status;
@@ -282,28 +283,32 @@ int configure_launch(qdfn_ctx* c) {
         ApplyKernel ka = apply_kernel(c->prec, c->R);
         QDFN_CUDA(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
     }
-    c->release(c->part_s);
-    c->release(c->part_n);
-    c->release(c->red);
-    c->part_s = c->part_n = nullptr;
+    // work buffers kept when large enough (a re-division of an ensemble's SMs
+    // re-sizes every member): every launch rewrites them before reading
+    auto ensure = [&](auto** ptr, size_t n, size_t& cap) -> int {
+        if (*ptr && cap >= n) return QDFN_OK;
+        c->release(*ptr);
+        *ptr = nullptr;
+        cap = n;
+        return c->dalloc(ptr, n);
+    };
     int rc;
     if (!c->hmat) {
-        c->release(c->xd);
-        c->xd = nullptr;
         // x copy of D: N columns padded to a multiple of 8 (+8), read in runs of 4
         // elements per x copy (two: current and next step), a multiple of 32 so
         // that the second copy starts 16-byte aligned like the first (bulk copies
         // need 16-byte aligned sources)
         c->xd_stride = (((int64_t)c->N + 16) * Rk + 31) / 32 * 32;
-        if ((rc = c->dalloc(reinterpret_cast<unsigned char**>(&c->xd), 2 * (size_t)c->xd_stride * xsz))) return rc;
+        if ((rc = ensure(reinterpret_cast<unsigned char**>(&c->xd), 2 * (size_t)c->xd_stride * xsz, c->xd_cap)))
+            return rc;
         if ((reinterpret_cast<uintptr_t>(c->xd) | (uintptr_t)(c->xd_stride * xsz)) % 16 != 0)
             return fail(QDFN_ERR_INVALID, "x copy of D not 16-byte aligned");
         const size_t slots = (size_t)std::max(c->nchunk, c->nchunk2);
         c->part_stride = (int64_t)slots * Rk * c->N;   // two buffers: this step's and the next's
-        if ((rc = c->dalloc(&c->part_s, 2 * (size_t)c->part_stride))) return rc;
-        if ((rc = c->dalloc(&c->part_n, 2 * (size_t)c->part_stride))) return rc;
+        if ((rc = ensure(&c->part_s, 2 * (size_t)c->part_stride, c->part_cap))) return rc;
+        if ((rc = ensure(&c->part_n, 2 * (size_t)c->part_stride, c->partn_cap))) return rc;
     }
-    if ((rc = c->dalloc(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots))) return rc;
+    if ((rc = ensure(&c->red, (size_t)2 * c->nblocks * Rk * kRedSlots, c->red_cap))) return rc;
     return QDFN_OK;
 }
 

@@ -35,6 +35,7 @@ EXPORTS = [
     "qdfn_ensemble_create", "qdfn_ensemble_destroy", "qdfn_ensemble_get_blocks", "qdfn_ensemble_set_blocks",
     "qdfn_ensemble_balance", "qdfn_ensemble_run", "qdfn_ensemble_run_async", "qdfn_ensemble_sync",
     "qdfn_ensemble_shares", "qdfn_ensemble_set_fill", "qdfn_check_division", "qdfn_adjoint_run",
+    "qdfn_assemble_tri_pairs_dev",
 ]
 
 
@@ -128,6 +129,8 @@ def load():
     L.qdfn_ensemble_shares.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p]
     L.qdfn_ensemble_set_fill.argtypes = [C.c_void_p, C.c_int]
     L.qdfn_check_division.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qdfn_assemble_tri_pairs_dev.argtypes = [C.c_int64] + [C.c_void_p] * 9 + [C.c_double, C.c_double] + \
+                                             [C.c_void_p] * 3
     L.qdfn_adjoint_run.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64] + [C.c_void_p] * 9 + \
                                   [C.c_double]
     _lib = L

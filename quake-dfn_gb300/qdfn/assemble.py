@@ -87,3 +87,22 @@ def assemble_tri_dev(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisso
                                        centre.shape[0], centre.data_ptr(), nhat.data_ptr(), shat.data_ptr(),
                                        float(shear_modulus), float(poisson), Ks.data_ptr(), Kn.data_ptr(),
                                        Ks.stride(0), lay, stream))
+
+
+def assemble_tri_pairs_dev(ridx, sidx, P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, stream=0):
+    """Gathered triangle stiffness entries (qdfn_assemble_tri_pairs_dev): ridx,
+    sidx int64 CUDA tensors of receiver and source indices into the per-triangle
+    float64 CUDA tensors; returns (Ks, Kn) CUDA tensors of the pairs."""
+    import torch
+    L = _lib.load()
+    n = int(ridx.shape[0])
+    Ks = torch.empty(n, dtype=torch.float64, device=ridx.device)
+    Kn = torch.empty(n, dtype=torch.float64, device=ridx.device)
+    for t in (ridx, sidx, P1, P2, P3, rake, centre, nhat, shat):
+        if not t.is_contiguous():
+            raise ValueError("assemble_tri_pairs_dev needs contiguous tensors")
+    _lib.check(L.qdfn_assemble_tri_pairs_dev(n, ridx.data_ptr(), sidx.data_ptr(), P1.data_ptr(), P2.data_ptr(),
+                                             P3.data_ptr(), rake.data_ptr(), centre.data_ptr(), nhat.data_ptr(),
+                                             shat.data_ptr(), float(shear_modulus), float(poisson), Ks.data_ptr(),
+                                             Kn.data_ptr(), stream))
+    return Ks, Kn

@@ -225,15 +225,16 @@ def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, devi
 
 
 def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6,
-              device="cuda"):
+              device="cuda", chunk=1 << 24):
     """Build the H-matrix of a triangular-patch system (TDstressHS kernels,
     StiffnessMatrix_ByParts_Calculation_Tri, scripts/Functions_BuildInputFile.jl:551-594,
-    in the block structure HmatBuild_T builds at :643-723).  Near-field blocks
-    are assembled densely on the GPU; admissible blocks are compressed by ACA
-    whose rows and columns are single receivers x a source range and a receiver
-    range x single sources of the assembly kernel -- no admissible block is ever
-    formed whole.  Returns (HMatrix, perm): block ranges index the permuted
-    ordering (every per-patch array [perm])."""
+    in the block structure HmatBuild_T builds at :643-723).  Entries are
+    formed on the GPU from index lists (qdfn_assemble_tri_pairs_dev): the
+    near-field blocks whole, in batches of `chunk` entries, and the admissible
+    blocks only where batched ACA asks for them (one row and one column per
+    block and iteration, every block in the same launches) -- no admissible
+    block is ever formed whole.  Returns (HMatrix, perm): block ranges index
+    the permuted ordering (every per-patch array [perm])."""
     import torch
     from . import assemble
     tree = ClusterTree(np.asarray(centre), leaf=leaf)
@@ -241,38 +242,190 @@ def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf
     dv = lambda a: torch.tensor(np.ascontiguousarray(np.asarray(a)[perm]), dtype=torch.float64,
                                 device=device)
     p1, p2, p3, rk, cen, nh, sh = (dv(a) for a in (P1, P2, P3, rake, centre, nhat, shat))
-    G, nu = shear_modulus, poisson
 
-    def block(s0, s1, r0, r1):
-        """(Ks, Kn) of receivers [r0, r1) x sources [s0, s1), each (recv x src)."""
-        ns, nr = s1 - s0, r1 - r0
-        Ks = torch.empty((ns, nr), dtype=torch.float64, device=device)
-        Kn = torch.empty((ns, nr), dtype=torch.float64, device=device)
-        assemble.assemble_tri_dev(p1[s0:s1], p2[s0:s1], p3[s0:s1], rk[s0:s1], cen[r0:r1], nh[r0:r1], sh[r0:r1],
-                                  G, nu, Ks, Kn, layout="col")
-        return Ks.T, Kn.T
+    def evaluate(ridx, sidx):
+        outs, outn = [], []
+        for k in range(0, int(ridx.shape[0]), chunk):
+            a, b = assemble.assemble_tri_pairs_dev(ridx[k:k + chunk].contiguous(), sidx[k:k + chunk].contiguous(),
+                                                   p1, p2, p3, rk, cen, nh, sh, shear_modulus, poisson)
+            outs.append(a)
+            outn.append(b)
+        if not outs:
+            z = torch.zeros(0, dtype=torch.float64, device=device)
+            return z, z
+        return torch.cat(outs), torch.cat(outn)
 
-    ranges, ds, us, vs, dn, un, vn = [], [], [], [], [], [], []
-    for (s, t, adm) in block_partition(tree, eta):
-        s0, s1 = tree.starts[s], tree.ends[s]
-        r0, r1 = tree.starts[t], tree.ends[t]
-        ns, nr = s1 - s0, r1 - r0
-        ranges.append((s0, s1 - 1, r0, r1 - 1))
-        if not adm:
-            Bs, Bn = block(s0, s1, r0, r1)
-            for B, Ul, Vl, Dl in ((Bs, us, vs, ds), (Bn, un, vn, dn)):
-                Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
-            continue
-        for side, (Ul, Vl, Dl) in enumerate(((us, vs, ds), (un, vn, dn))):
-            row = lambda i: block(s0, s1, r0 + i, r0 + i + 1)[side][0].clone()
-            col = lambda j: block(s0 + j, s0 + j + 1, r0, r1)[side][:, 0].clone()
-            U, Vt = aca_fn(row, col, nr, ns, tol, max_rank=MAX_RANK, device=device, dtype=torch.float64)
-            if U.shape[1] < MAX_RANK and U.shape[1] * (nr + ns) < nr * ns:
-                Ul.append(U.cpu().numpy()); Vl.append(Vt.cpu().numpy()); Dl.append(None)
-            else:
-                B = block(s0, s1, r0, r1)[side]
-                Ul.append(None); Vl.append(None); Dl.append(B.contiguous().cpu().numpy())
-    return HMatrix(np.array(ranges, dtype=np.int64), ds, us, vs, dn, un, vn, perm), perm
+    def dense_blocks(bl):
+        """(recv x src) host arrays of both matrices for blocks (s0, s1, r0, r1)."""
+        res = []
+        for k0 in range(0, len(bl), 256):
+            part = bl[k0:k0 + 256]
+            rr, ss = [], []
+            for (s0, s1, r0, r1) in part:
+                r = torch.arange(r0, r1, device=device)
+                c = torch.arange(s0, s1, device=device)
+                rr.append(r.repeat_interleave(s1 - s0))
+                ss.append(c.repeat(r1 - r0))
+            Ks, Kn = evaluate(torch.cat(rr), torch.cat(ss))
+            Ks, Kn = Ks.cpu().numpy(), Kn.cpu().numpy()
+            off = 0
+            for (s0, s1, r0, r1) in part:
+                n = (s1 - s0) * (r1 - r0)
+                res.append((Ks[off:off + n].reshape(r1 - r0, s1 - s0), Kn[off:off + n].reshape(r1 - r0, s1 - s0)))
+                off += n
+        return res
+
+    parts = block_partition(tree, eta)
+    spans = [(tree.starts[s], tree.ends[s], tree.starts[t], tree.ends[t]) for (s, t, _) in parts]
+    near = [k for k, (_, _, adm) in enumerate(parts) if not adm]
+    far = [k for k, (_, _, adm) in enumerate(parts) if adm]
+    nb = len(parts)
+    ds, us, vs, dn, un, vn = ([None] * nb for _ in range(6))
+    for k, (Bs, Bn) in zip(near, dense_blocks([spans[k] for k in near])):
+        ds[k], dn[k] = Bs, Bn
+    if far:
+        nr = [spans[k][3] - spans[k][2] for k in far]
+        ns = [spans[k][1] - spans[k][0] for k in far]
+        (fs, fn), ro, co = aca_batched(nr, ns, [spans[k][2] for k in far], [spans[k][0] for k in far], evaluate,
+                                       tol)
+        redo = []
+        for j, k in enumerate(far):
+            for (U, V, rank), Ul, Vl, side in ((fs, us, vs, 0), (fn, un, vn, 1)):
+                rk_b = int(rank[j])
+                if rk_b < MAX_RANK and rk_b * (nr[j] + ns[j]) < nr[j] * ns[j]:
+                    Ul[k] = np.ascontiguousarray(U[ro[j]:ro[j] + nr[j], :rk_b])
+                    Vl[k] = np.ascontiguousarray(V[:rk_b, co[j]:co[j] + ns[j]])
+                else:
+                    redo.append((k, side))
+        if redo:   # not worth compressing (or not converged at the rank limit): stored dense
+            for (k, side), (Bs, Bn) in zip(redo, dense_blocks([spans[k] for k, _ in redo])):
+                if side == 0:
+                    ds[k] = Bs
+                else:
+                    dn[k] = Bn
+    ranges = np.array([(s0, s1 - 1, r0, r1 - 1) for (s0, s1, r0, r1) in spans], dtype=np.int64)
+    return HMatrix(ranges, ds, us, vs, dn, un, vn, perm), perm
+
+
+def _seg_argmax(vals, seg, nseg):
+    """Per segment: the largest value and the first flat index holding it
+    (vals float64 CUDA tensor, seg its segment ids)."""
+    import torch
+    m = torch.full((nseg,), -float("inf"), dtype=vals.dtype, device=vals.device)
+    m = m.scatter_reduce(0, seg, vals, reduce="amax", include_self=True)
+    n = vals.shape[0]
+    idx = torch.arange(n, device=vals.device)
+    cand = torch.where(vals == m[seg], idx, torch.full_like(idx, n))
+    first = torch.full((nseg,), n, dtype=idx.dtype, device=vals.device)
+    first = first.scatter_reduce(0, seg, cand, reduce="amin", include_self=True)
+    return m, first
+
+
+def _seg_sum(vals, seg, nseg):
+    import torch
+    return torch.zeros(nseg, dtype=vals.dtype, device=vals.device).index_add_(0, seg, vals)
+
+
+def aca_batched(nr, ns, r0, s0, evaluate, tol, max_rank=MAX_RANK):
+    """ACA with partial pivoting on many blocks at once, both matrices of the
+    pair (shear, normal) with their own pivots: every iteration asks
+    `evaluate(recv, src) -> (Ks, Kn)` (CUDA index tensors, global indices) for
+    one row of each active block and side, then one column -- two gathered
+    kernel launches per iteration for all blocks together.  Returns, per
+    side, the host arrays U (sum nr x rank_max), V (rank_max x sum ns) and the
+    per-block ranks; block b's factors are U[ro_b:ro_b+nr_b, :rank_b] and
+    V[:rank_b, co_b:co_b+ns_b] (ro, co the exclusive prefix sums of nr, ns)."""
+    import torch
+    dev = "cuda"
+    B = len(nr)
+    nr_t = torch.tensor(nr, dtype=torch.int64, device=dev)
+    ns_t = torch.tensor(ns, dtype=torch.int64, device=dev)
+    r0_t = torch.tensor(r0, dtype=torch.int64, device=dev)
+    s0_t = torch.tensor(s0, dtype=torch.int64, device=dev)
+    ro = torch.cumsum(nr_t, 0) - nr_t
+    co = torch.cumsum(ns_t, 0) - ns_t
+    Tr, Tc = int(nr_t.sum()), int(ns_t.sum())
+    rblk = torch.repeat_interleave(torch.arange(B, device=dev), nr_t)
+    cblk = torch.repeat_interleave(torch.arange(B, device=dev), ns_t)
+    rloc = torch.arange(Tr, device=dev) - ro[rblk]
+    cloc = torch.arange(Tc, device=dev) - co[cblk]
+    out = []
+    sides = [dict(active=torch.ones(B, dtype=torch.bool, device=dev), piv=torch.zeros(B, dtype=torch.int64, device=dev),
+                  used=torch.zeros(Tr, dtype=torch.bool, device=dev), frob2=torch.zeros(B, dtype=torch.float64,
+                                                                                        device=dev),
+                  rank=torch.zeros(B, dtype=torch.int64, device=dev), U=[], V=[]) for _ in range(2)]
+    for it in range(max_rank):
+        if not any(bool(sd["active"].any()) for sd in sides):
+            break
+        # rows: the pivot row of every active block, for both sides in one launch
+        rr, ss, parts = [], [], []
+        for sd in sides:
+            m = sd["active"][cblk]
+            ic = torch.nonzero(m).flatten()
+            b = cblk[ic]
+            rr.append(r0_t[b] + sd["piv"][b])
+            ss.append(s0_t[b] + cloc[ic])
+            parts.append(ic)
+        Ks, Kn = evaluate(torch.cat(rr), torch.cat(ss))
+        off = 0
+        cols = []
+        for side, sd in enumerate(sides):
+            ic = parts[side]
+            vals = (Ks if side == 0 else Kn)[off:off + ic.shape[0]]
+            off += ic.shape[0]
+            R = torch.zeros(Tc, dtype=torch.float64, device=dev)
+            R[ic] = vals
+            for Ul, Vl in zip(sd["U"], sd["V"]):
+                R -= Ul[ro + sd["piv"]][cblk] * Vl
+            act_c = sd["active"][cblk]
+            absR = torch.where(act_c, R.abs(), torch.full_like(R, -1.0))
+            mx, jf = _seg_argmax(absR, cblk, B)
+            jf = torch.clamp(jf, max=Tc - 1)
+            piv = R[jf]
+            ok = sd["active"] & (mx > 0)
+            sd["active"] = ok
+            sd["jf"] = jf
+            sd["v"] = torch.where(ok[cblk], R / torch.where(ok, piv, torch.ones_like(piv))[cblk], torch.zeros_like(R))
+            m = ok[rblk]
+            ir = torch.nonzero(m).flatten()
+            b = rblk[ir]
+            cols.append((ir, r0_t[b] + rloc[ir], s0_t[b] + (jf[b] - co[b])))
+        Ks, Kn = evaluate(torch.cat([c[1] for c in cols]), torch.cat([c[2] for c in cols]))
+        off = 0
+        for side, sd in enumerate(sides):
+            ir = cols[side][0]
+            vals = (Ks if side == 0 else Kn)[off:off + ir.shape[0]]
+            off += ir.shape[0]
+            u = torch.zeros(Tr, dtype=torch.float64, device=dev)
+            u[ir] = vals
+            jf = sd["jf"]
+            for Ul, Vl in zip(sd["U"], sd["V"]):
+                u -= Vl[jf][rblk] * Ul
+            act_r = sd["active"][rblk]
+            u = torch.where(act_r, u, torch.zeros_like(u))
+            v = sd["v"]
+            nu2 = _seg_sum(u * u, rblk, B) * _seg_sum(v * v, cblk, B)
+            cross = torch.zeros(B, dtype=torch.float64, device=dev)
+            for Ul, Vl in zip(sd["U"], sd["V"]):
+                cross += _seg_sum(u * Ul, rblk, B) * _seg_sum(v * Vl, cblk, B)
+            sd["frob2"] = sd["frob2"] + torch.where(sd["active"], nu2 + 2 * cross, torch.zeros_like(nu2))
+            sd["U"].append(u)
+            sd["V"].append(v)
+            sd["rank"] += sd["active"].to(torch.int64)
+            conv = nu2 <= (tol ** 2) * torch.clamp(sd["frob2"], min=1e-300)
+            # next pivot row: the largest |u| among the rows not used yet
+            sd["used"] = sd["used"] | torch.zeros_like(sd["used"]).index_fill_(0, ro + sd["piv"], True) & \
+                sd["active"][rblk]
+            cand = torch.where(sd["used"] | ~act_r, torch.full_like(u, -1.0), u.abs())
+            mx, nxt = _seg_argmax(cand, rblk, B)
+            sd["piv"] = torch.where(mx >= 0, torch.clamp(nxt, max=Tr - 1) - ro, sd["piv"])
+            sd["active"] = sd["active"] & ~conv & (mx >= 0)
+    for sd in sides:
+        k = len(sd["U"])
+        U = torch.stack(sd["U"], 1).cpu().numpy() if k else np.zeros((Tr, 0))
+        V = torch.stack(sd["V"], 0).cpu().numpy() if k else np.zeros((0, Tc))
+        out.append((U, V, sd["rank"].cpu().numpy()))
+    return out, ro.cpu().numpy(), co.cpu().numpy()
 
 
 def set_hmatrix(sim, H, precision="fp64"):

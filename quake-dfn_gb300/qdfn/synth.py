@@ -160,3 +160,59 @@ def problem_dict(sys, kself_diag, switch_v=1e-2, dt_cut=5.0, rupture_multiple=3.
         for k in ("a", "b", "Dc", "theta_i", "V_i", "f_i"):
             p[k] = np.tile(p[k], n_inst)
     return p
+
+
+def curved_fault_network(seed=0, n_faults=5, length=8000.0, width=4000.0, edge=80.0, amplitude=200.0, G=32e9,
+                         nu=0.25, top=500.0, spacing=3000.0):
+    """Triangulated curved faults (the triangle-mesh configuration): n_faults
+    surfaces of length x width (along strike x down dip), each the plane
+    through its trace bent out of plane by w(u, v) = sum of 3 sinusoids of
+    amplitude `amplitude` and random wavelengths and phases, meshed at `edge`
+    into 2 triangles per grid cell; near-parallel strikes (a random base
+    strike +- 5 degrees), dips U[70, 90], traces `spacing` apart, tops `top`
+    below the surface.  Friction as in
+    fault_network.  Returns the 20-column triangle bulk table (P1, P2, P3,
+    rake, ...) and the per-triangle problem fields."""
+    rng = np.random.default_rng(seed)
+    nu_c, nv_c = int(round(length / edge)), int(round(width / edge))
+    tris = []
+    base = rng.uniform(0.0, 180.0)
+    n_base = np.array([-sind(base), cosd(base), 0.0])
+    s_base = np.array([cosd(base), sind(base), 0.0])
+    for f in range(n_faults):
+        # near-parallel strands `spacing` apart (strikes within 5 degrees, so no two surfaces meet)
+        strike = base + rng.uniform(-5.0, 5.0)
+        dip = rng.uniform(70.0, 90.0)
+        k = 2 * np.pi / rng.uniform(2000.0, 8000.0, 3)
+        phase = rng.uniform(0.0, 2 * np.pi, (3, 2))
+        origin = (f - (n_faults - 1) / 2) * spacing * n_base + rng.uniform(-1000.0, 1000.0) * s_base
+        us = np.array([cosd(strike), sind(strike), 0.0])                          # along strike
+        nh = np.array([-sind(strike), cosd(strike), 0.0])                         # horizontal normal
+        ud = cosd(dip) * nh + np.array([0.0, 0.0, -sind(dip)])                    # down dip (z up)
+        nrm = np.cross(us, ud)
+        uu = np.linspace(-length / 2, length / 2, nu_c + 1)
+        vv = np.linspace(0.0, width, nv_c + 1)
+        U, Vv = np.meshgrid(uu, vv, indexing="ij")
+        w = sum(amplitude / 3 * np.sin(k[i] * U + phase[i, 0]) * np.cos(k[i] * Vv + phase[i, 1]) for i in range(3))
+        P = origin + U[..., None] * us + Vv[..., None] * ud + w[..., None] * nrm
+        P[..., 2] -= top
+        for i in range(nu_c):
+            for j in range(nv_c):
+                a, b, c, d = P[i, j], P[i + 1, j], P[i + 1, j + 1], P[i, j + 1]
+                tris.append((a, b, c))
+                tris.append((a, c, d))
+    n = len(tris)
+    seg = np.zeros((n, 20))
+    for t, (a, b, c) in enumerate(tris):
+        seg[t, 0:3], seg[t, 3:6], seg[t, 6:9] = a, b, c
+    seg[:, 9] = 0.0                       # rake
+    a = rng.uniform(0.008, 0.012, n)
+    bb = a + rng.uniform(-0.004, 0.004, n)
+    Dc = 10 ** rng.uniform(-4, -2, n)
+    V_i = np.full(n, 1e-9)
+    depth = -(seg[:, 2] + seg[:, 5] + seg[:, 8]) / 3
+    rho = G / CS ** 2
+    return dict(seg=seg, N=n, Nload=0, G=G, nu=nu, rho=rho, a=a, b=bb, Dc=Dc, theta_i=Dc / V_i, V_i=V_i,
+                f_i=_friction_f0(a, bb, V_i), sigma0=18e6 * depth / 1000.0, V_const=np.zeros(n),
+                mass=np.full(n, edge * rho / 2), sigma_min=1e6, years=100.0, stressing_rate=0.01e6,
+                n_faults=n_faults, seed=seed)

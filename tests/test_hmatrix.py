@@ -93,7 +93,7 @@ def test_hmatrix_trajectory_matches_oracle(qdfn_mod, oracle_mod):
         assert np.max(np.abs(st["D"] - o.state["D"])) / np.max(np.abs(o.state["D"])) < tol
 
 
-def _tri_system(nx=16, ny=10, seed=1):
+def _tri_system(nx=32, ny=20, seed=1):
     from qdfn import geometry
     from _systems import bumpy_triangles
     seg = bumpy_triangles(nx=nx, ny=ny, seed=seed)
@@ -104,7 +104,7 @@ def _tri_system(nx=16, ny=10, seed=1):
 
 @pytest.mark.gpu
 def test_triangle_hmatrix_aca_on_demand_matches_dense_and_oracle(qdfn_mod, oracle_mod):
-    """A curved triangulated fault (320 TDstressHS elements, leaf 16, eta 2):
+    """A curved triangulated fault (1,280 TDstressHS elements, leaf 32, eta 2):
     ACA forms its rows and columns from the triangle kernel on index ranges (no
     admissible block assembled whole); the compressed operator equals the dense
     triangle operator to the ACA tolerance, and the device H product (warp tasks)
@@ -113,7 +113,7 @@ def test_triangle_hmatrix_aca_on_demand_matches_dense_and_oracle(qdfn_mod, oracl
     from qdfn import assemble, hmatrix, simulate
     P1, P2, P3, rake, cen, un, us = _tri_system()
     N = P1.shape[0]
-    H, perm = hmatrix.build_tri(P1, P2, P3, rake, cen, un, us, G, NU, leaf=16, eta=2.0, tol=1e-8)
+    H, perm = hmatrix.build_tri(P1, P2, P3, rake, cen, un, us, G, NU, leaf=32, eta=2.0, tol=1e-8)
     assert any(U is not None for U in H.U_s) and H.stored_entries() < 2 * N * N
     Ks, Kn = assemble.assemble_tri(P1[perm], P2[perm], P3[perm], rake[perm], cen[perm], un[perm], us[perm], G, NU)
     Hs, Hn = H.to_dense(N)
