@@ -169,7 +169,7 @@ def curved_fault_network(seed=0, n_faults=5, length=8000.0, width=4000.0, edge=8
     through its trace bent out of plane by w(u, v) = sum of 3 sinusoids of
     amplitude `amplitude` and random wavelengths and phases, meshed at `edge`
     into 2 triangles per grid cell; near-parallel strikes (a random base
-    strike +- 5 degrees), dips U[70, 90], traces `spacing` apart, tops `top`
+    strike +- 5 degrees), dips U[70, 85], traces `spacing` apart, tops `top`
     below the surface.  Friction as in
     fault_network.  Returns the 20-column triangle bulk table (P1, P2, P3,
     rake, ...) and the per-triangle problem fields."""
@@ -182,7 +182,9 @@ def curved_fault_network(seed=0, n_faults=5, length=8000.0, width=4000.0, edge=8
     for f in range(n_faults):
         # near-parallel strands `spacing` apart (strikes within 5 degrees, so no two surfaces meet)
         strike = base + rng.uniform(-5.0, 5.0)
-        dip = rng.uniform(70.0, 90.0)
+        # dips below 85 degrees: a TD side along the vertical is a singular
+        # configuration of the angular dislocations
+        dip = rng.uniform(70.0, 85.0)
         k = 2 * np.pi / rng.uniform(2000.0, 8000.0, 3)
         phase = rng.uniform(0.0, 2 * np.pi, (3, 2))
         origin = (f - (n_faults - 1) / 2) * spacing * n_base + rng.uniform(-1000.0, 1000.0) * s_base

@@ -1,8 +1,8 @@
 """The mixed-precision contract against the FP64 oracle: with the elastic
 operator stored in FP32 (FP64 state, friction inversion, time and step
 control), the relative slip error max|D - D_oracle| / max|D_oracle| stays at
-or below 1e-6, and simulated time within 1e-6, at every recorded step of the
-interseismic horizon -- until the first patch accelerates past twice the
+or below 1e-6 at matched simulated times (every oracle step of the
+interseismic horizon, the GPU slip interpolated in time) -- until the first patch accelerates past twice the
 largest starting slip rate (the onset of nucleation).  From there on the trajectories are
 unstable: a nucleating patch's slip-rate runaway amplifies any perturbation
 exponentially (a 1e-15 perturbation of the FP64 operator already grows to
@@ -29,11 +29,26 @@ def pre_nucleation_records(hist, ns, v_start, factor=2.0):
     return int(bad[0]) if bad.size else int(vmax.shape[0])
 
 
-def _compare(gh, oh, n):
-    """Relative slip error and relative time error over the first n records."""
-    d = float(np.max(np.abs(gh["D"][:n] - oh["D"][:n])) / max(np.max(np.abs(oh["D"][:n])), 1e-300))
-    t = float(np.max(np.abs(gh["T"][:n] / oh["T"][:n] - 1)))
-    return d, t
+def matched_time_err(gh, oh, n):
+    """Relative slip error at matched simulated times (the reference records on
+    step counts, and the two runs' adaptive steps may differ in the last bits,
+    or by a branch of the step control): the GPU history's slip interpolated
+    linearly in time at each of the first n oracle record times, against the
+    oracle's, over max |D_oracle| of those records."""
+    Tg, Dg = gh["T"], gh["D"]
+    err = 0.0
+    for j in range(n):
+        t = oh["T"][j]
+        k = int(np.searchsorted(Tg, t))
+        if k == 0:
+            d = Dg[0] if t == Tg[0] else Dg[0] * (t / Tg[0])   # before the first record: from D = 0 at T = 0
+        elif k >= len(Tg):
+            return float("inf")                              # past the GPU's window
+        else:
+            w = (t - Tg[k - 1]) / (Tg[k] - Tg[k - 1])
+            d = Dg[k - 1] + w * (Dg[k] - Dg[k - 1])
+        err = max(err, float(np.max(np.abs(d - oh["D"][j]))))
+    return err / max(float(np.max(np.abs(oh["D"][:n]))), 1e-300)
 
 
 def _oracle(oracle_mod, prob, ext, op, nsteps, rstep, r=None):
@@ -55,7 +70,7 @@ def test_c1_single_fault_fp32_within_1e6_of_the_oracle(qdfn_mod, oracle_mod):
     Ks, Kn = assemble.assemble_rect(rec, rec, sysd["G"], sysd["nu"])
     prob = synth.problem_dict(sysd, np.diag(Ks))
     ext = synth.external_ramp(sysd["N"], sysd["stressing_rate"], 1e12)
-    steps, rstep = 300, 2
+    steps, rstep = 300, 1
     oh = _oracle(oracle_mod, prob, ext, ("dense", Ks, Kn), steps, rstep)
     n = pre_nucleation_records(oh, sysd["N"], np.max(prob["V_i"]))
     assert n * rstep >= 40, n * rstep
@@ -63,8 +78,8 @@ def test_c1_single_fault_fp32_within_1e6_of_the_oracle(qdfn_mod, oracle_mod):
     sim.set_dense(Ks, Kn, "fp32")
     sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
     sim.run(steps, timeout_s=120)
-    d, t = _compare(sim.history(0), oh, n)
-    assert d <= 1e-6 and t <= 1e-6, (d, t, n)
+    d = matched_time_err(sim.history(0), oh, n)
+    assert d <= 1e-6, (d, n)
     sim.close()
 
 
@@ -88,7 +103,7 @@ def test_reduced_network_four_draws_within_bound_of_the_oracle(qdfn_mod, oracle_
     from qdfn import simulate
     sysd, rec, Ks, Kn, prob, ext = _network()
     N = sysd["N"]
-    steps, rstep = 400, 5
+    steps, rstep = 400, 1
     sim = simulate.Simulation(prob, n_inst=4, record_step=rstep, max_records=steps // rstep)
     sim.set_dense(Ks, Kn, precision)
     sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
@@ -99,8 +114,7 @@ def test_reduced_network_four_draws_within_bound_of_the_oracle(qdfn_mod, oracle_
         n = pre_nucleation_records(oh, N - sysd["Nload"], np.max(prob["V_i"]))
         horizons.append(n * rstep)
         if n:
-            d, t = _compare(sim.history(r), oh, n)
-            worst = max(worst, d, t)
+            worst = max(worst, matched_time_err(sim.history(r), oh, n))
     assert sorted(horizons)[1] >= 40, horizons        # at least three draws compared over >= 40 steps
     assert worst <= bound, (worst, horizons)
     sim.close()
@@ -120,7 +134,7 @@ def test_hmatrix_fp32_within_1e6_of_the_oracle_h_product(qdfn_mod, oracle_mod):
     prob = problem_for(recp, Hs, seed=3)
     prob["interp_at_told"] = 1
     ext = synth.external_ramp(rec.shape[0], 1e6, 1e11)
-    steps, rstep = 300, 5
+    steps, rstep = 300, 1
     blocks = dict(range=H.ranges, sD=H.dense_s, sU=H.U_s, sVt=H.Vt_s, nD=H.dense_n, nU=H.U_n, nVt=H.Vt_n)
     oh = _oracle(oracle_mod, prob, ext, ("hmat", blocks), steps, rstep)
     n = pre_nucleation_records(oh, rec.shape[0], np.max(prob["V_i"]))
@@ -129,6 +143,6 @@ def test_hmatrix_fp32_within_1e6_of_the_oracle_h_product(qdfn_mod, oracle_mod):
     hmatrix.set_hmatrix(sim, H, "fp32")
     sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
     sim.run(steps, timeout_s=120)
-    d, t = _compare(sim.history(0), oh, n)
-    assert d <= 1e-6 and t <= 1e-6, (d, t, n)
+    d = matched_time_err(sim.history(0), oh, n)
+    assert d <= 1e-6, (d, n)
     sim.close()

@@ -43,3 +43,25 @@ def test_external_ramp_layout():
     assert e["t"].tolist() == [0.0, 1e12]
     assert e["shear"].shape == (2, 5) and np.all(e["shear"][0] == 0)
     assert np.allclose(e["shear"][1], 0.01e6 * 1e12 / (365.25 * 86400.0))
+
+
+def test_curved_fault_network_shapes(oracle_mod):
+    """The triangle-mesh workload: 5 near-parallel curved faults of 8 x 4 km
+    (edge 400 m here: 2 x 20 x 10 triangles each), every vertex below the
+    surface, every self stiffness negative (the oracle's TDstressHS), friction
+    in the network's ranges."""
+    import numpy as np
+    from qdfn import synth
+    d = synth.curved_fault_network(seed=2, edge=400.0)
+    seg = d["seg"]
+    assert d["N"] == seg.shape[0] == 5 * 2 * 20 * 10 and seg.shape[1] == 20
+    assert np.max(seg[:, [2, 5, 8]]) < 0
+    assert np.all((d["a"] >= 0.008) & (d["a"] <= 0.012)) and np.all(np.abs(d["b"] - d["a"]) <= 0.004)
+    assert np.all(d["sigma0"] > 0)
+    from qdfn import geometry
+    P1, P2, P3, un, _, _, us = geometry.rot_verts_unit_vectors_abi(seg, seg[:, 9])
+    c = (P1 + P2 + P3) / 3
+    for i in range(0, d["N"], 7):
+        Ks, _ = oracle_mod.assemble_tri(P1[i:i + 1], P2[i:i + 1], P3[i:i + 1], seg[i:i + 1, 9], c[i:i + 1],
+                                        un[i:i + 1], us[i:i + 1], d["G"], d["nu"], nthreads=1)
+        assert Ks[0, 0] < 0, i
