@@ -59,13 +59,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="ensemble", choices=["network", "ensemble", "tri_h"],
+    ap.add_argument("--workload", default="ensemble", choices=["network", "ensemble", "tri_h", "adjoint"],
                     help="ensemble (default, C4): 64 fault networks of 800-6,000 patches x 4 friction draws in "
                          "one persistent launch; network (C2): the 30-fault network x 4 draws")
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--cpu-members", type=int, default=4,
                     help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
-    ap.add_argument("--rebalance-every", type=int, default=250,
+    ap.add_argument("--rebalance-every", type=int, default=100,
                     help="ensemble: steps per launch in the timed window, the SMs re-divided between launches "
                          "(0: one launch)")
     ap.add_argument("--no-fill", dest="fill", action="store_false",
@@ -1082,6 +1082,68 @@ def run_tri_h(args):
     print(json.dumps(line))
 
 
+def run_adjoint(args):
+    """C5: gradient of a trajectory loss with respect to every patch's a, b and
+    Dc on the fault network (seed 2, 30 faults, 12,813 patches, one friction
+    draw), operator in FP32 (--precision fp64 for the all-FP64 adjoint): the
+    forward window of K steps (one step per launch, sqrt(K) checkpoints) and the
+    reverse sweep through qdfn_adjoint_run.  Loss: squared misfit of the final
+    slip against a run with 1 %-perturbed a, b, Dc.  Reports the wall time of
+    forward + reverse against the plain forward (one persistent launch)."""
+    import torch
+    from qdfn import adjoint, assemble, simulate
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    sysd, _ = workload(args)
+    N = sysd["N"]
+    rec = torch.tensor(sysd["records"], dtype=torch.float64, device=dev)
+    Ks = torch.empty((N, N), dtype=torch.float64, device=dev)
+    Kn = torch.empty((N, N), dtype=torch.float64, device=dev)
+    assemble.assemble_rect_dev(rec, rec, sysd["G"], sysd["nu"], Ks, Kn, layout="col")
+    kdiag = torch.diagonal(Ks).cpu().numpy()
+    prob = problem(sysd, None, kdiag, 1)
+    ext = ext_ramp(sysd)
+    rng = np.random.default_rng(11)
+    pert = dict(prob)
+    for k in ("a", "b", "Dc"):
+        pert[k] = prob[k] * (1 + 0.01 * rng.standard_normal(N))
+
+    def make(p):
+        sim = simulate.Simulation(p)
+        sim.set_dense_device(Ks, Kn, args.precision, layout="col")
+        sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+        return sim
+
+    tgt = make(pert)
+    tgt.run(args.steps, timeout_s=TIMEOUT)
+    Dstar = tgt.state(0)["D"]
+    tgt.close()
+    fwd = make(prob)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fwd.run(args.steps, timeout_s=TIMEOUT)
+    t_fwd = time.perf_counter() - t0
+    D = fwd.state(0)["D"]
+    yrs = fwd.state(0)["T"] / YEAR
+    fwd.close()
+    sim = make(prob)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = adjoint.gradient(sim, args.steps, dL_dD_final=2 * (D - Dstar), timeout_s=TIMEOUT)
+    t_adj = time.perf_counter() - t0
+    sim.close()
+    line = {"metric": "adjoint wall time (forward + reverse), fault network", "value": t_adj, "unit": "s",
+            "n_gpus": 1, "steps": args.steps, "warmup": 0, "ms_per_step": t_adj / args.steps * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "%s-operator/fp64-state" % args.precision, "data": "synthetic (seeded fault network)",
+            "config": {"workload": "C5: fault network seed %d, %d rectangular patches, %d adaptive steps, gradients "
+                                   "of final-slip misfit w.r.t. a, b, Dc (every patch)" % (args.seed, N, args.steps),
+                       "patches": N, "checkpoints": int(np.ceil(np.sqrt(args.steps)))},
+            "forward_only_s": t_fwd, "adjoint_over_forward": t_adj / t_fwd, "sim_years_in_window": yrs,
+            "gradient_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1090,6 +1152,8 @@ def main():
         run_ensemble(args)
     elif args.workload == "tri_h":
         run_tri_h(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

@@ -47,6 +47,8 @@ struct qdfn_ctx {
     std::vector<void*> allocs;
     double *a, *b, *Dc, *F0, *tau0, *sigma0, *Vconst, *mass, *omega, *kself;
     double *la = nullptr, *lth0 = nullptr;   // ln(V_i/V0), ln(theta_i V0/Dc): F0's derivatives (adjoint)
+    double* dref = nullptr;                   // [2][R] reference slip of the FP32/BF16 x copy
+    double *rowsum_e = nullptr, *rowsum_n = nullptr;   // [N] row sums of the stored FP32/BF16 operator
     unsigned char* sw_used = nullptr;         // adjoint recording: solver of each patch in the next launch
     double *ra = nullptr, *rDc = nullptr;
     unsigned char* unstable;
@@ -132,6 +134,10 @@ SimParams make_params(qdfn_ctx* c, uint64_t budget_ns) {
     p.N = c->N; p.Nload = c->Nload; p.ld = c->ld; p.R = kernel_R(c->R);
     p.nblk = c->nblocks;
     p.sw_used = c->sw_used;
+    p.dref = c->dref;
+    const bool offs = !c->hmat && c->prec != QDFN_FP64 && c->rowsum_e;
+    p.rowsum_e = offs ? c->rowsum_e : nullptr;
+    p.rowsum_n = offs ? c->rowsum_n : nullptr;
     p.evolution_dr = c->prob.evolution_dr; p.interp_at_told = c->prob.interp_at_told; p.hmat = c->hmat;
     p.eta = c->eta; p.sigma_min = c->prob.sigma_min; p.switch_v = c->prob.switch_v;
     p.dt_cut = c->prob.dt_cut; p.rupture_dt = c->prob.rupture_dt; p.max_dt = c->prob.max_dt;
@@ -336,7 +342,7 @@ extern "C" int qdfn_ctx_create(qdfn_ctx** out, const qdfn_problem* pr) {
     A(a, RN); A(b, RN); A(Dc, RN); A(F0, RN); A(tau0, RN); A(sigma0, RN); A(Vconst, RN);
     A(ra, RN); A(rDc, RN);
     A(mass, RN); A(omega, RN); A(kself, (size_t)N); A(unstable, RN); A(has_unstable, (size_t)Rk);
-    A(la, RN); A(lth0, RN);
+    A(la, RN); A(lth0, RN); A(dref, 2 * (size_t)Rk);
     // the six host-visible state fields in one block, in the order of the
     // state-transfer calls, so that contiguous host buffers move in one copy
     double* state6 = nullptr;
@@ -463,6 +469,15 @@ int set_dense_device(qdfn_ctx* c, const double* dKs, const double* dKn, int64_t 
     dim3 grid((unsigned)((nrows + 255) / 256), (unsigned)std::min<int64_t>(N, 65535));
     k_convert<<<grid, 256, 0, st>>>(dKs, dKn, N, ld_in, layout, c->ld, precision, c->E, c->Kn, c->kself);
     QDFN_CUDA(cudaGetLastError());
+    c->release(c->rowsum_e);
+    c->release(c->rowsum_n);
+    c->rowsum_e = c->rowsum_n = nullptr;
+    if (precision != QDFN_FP64) {   // the x copy's offset needs the stored matrices' row sums
+        if ((rc = c->dalloc(&c->rowsum_e, (size_t)N)) || (rc = c->dalloc(&c->rowsum_n, (size_t)N))) return rc;
+        k_rowsum<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, c->ld, precision, c->E, c->Kn, c->rowsum_e,
+                                                              c->rowsum_n);
+        QDFN_CUDA(cudaGetLastError());
+    }
     QDFN_CUDA(cudaStreamSynchronize(st));
     // Omega = sqrt(K_Self / M) (Main_D :56); K_ii = 0 cannot normalise a row
     std::vector<double> ks(N), m((size_t)kernel_R(c->R) * N), om(m.size());

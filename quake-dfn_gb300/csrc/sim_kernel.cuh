@@ -137,6 +137,13 @@ struct SimParams {
     // adjoint recording (null: off): the solver each patch's accepted pass
     // used, [R][N] (0 low velocity, 1 high velocity, 2 loading fault)
     unsigned char* sw_used;
+    // FP32/BF16 dense operator: the x copy of D holds D - dref (dref = slip of
+    // patch 0 at the start of the step before, per instance, [2][R] by step
+    // parity), and the products add dref x the stored matrices' row sums
+    // (FP64, [N]; null for FP64 storage) -- the rounding of x to FP32 then
+    // scales with the slip's spread over the patches, not with the slip
+    double* dref;
+    const double *rowsum_e, *rowsum_n;
     unsigned long long* tmax;        // [kSets][4] per-step max over blocks of (operator end, solver end,
                                      // chunk ready->solved, last row block complete), ns
 };
@@ -1064,7 +1071,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             const int64_t i = q - (int64_t)r * N;
             const double Vo = p.V[q];
             p.sw[q] = Vo > p.switch_v ? 1 : 0;
-            if constexpr (!HM) reinterpret_cast<X*>(p.xd)[i * R + r] = (X)p.D[q];
+            if constexpr (!HM) {
+                const double d0 = (sizeof(X) == 4 && p.rowsum_e) ? p.D[(int64_t)r * N] : 0.0;
+                reinterpret_cast<X*>(p.xd)[i * R + r] = (X)(p.D[q] - d0);
+            }
             const bool ctl = p.has_unstable[r] ? (p.unstable[q] != 0) : (i < Ns);
             if (ctl) {
                 if (isnan(Vo)) v[r][1] = 1;
@@ -1085,6 +1095,8 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             }
             if (blk == 0 && HM) atomicExch(p.tile_ctr, 0ull);
         }
+        if (!HM && sizeof(X) == 4 && p.rowsum_e && blk == 0 && threadIdx.x < R)
+            p.dref[threadIdx.x] = p.D[(int64_t)threadIdx.x * N];   // step 0's offset
         if (!HM && blk == 0) {   // the counter sets of steps 0 and 1
             reset_counter_set(p, 0, true, threadIdx.x, blockDim.x);
             reset_counter_set(p, 1, true, threadIdx.x, blockDim.x);
@@ -1122,6 +1134,11 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             if (s_fill_stop) break;
         }
         const int par = s_par;             // which buffer holds the current state
+        // the next step's offset: this state's slip of patch 0 (the x copy this
+        // step's solves write holds D_next - dref_next)
+        const bool offs = !HM && sizeof(X) == 4 && p.rowsum_e != nullptr;
+        if (offs && blk == 0 && threadIdx.x < R)
+            p.dref[((it + 1) & 1) * R + threadIdx.x] = (par ? p.Dn : p.D)[(int64_t)threadIdx.x * N];
         const int cpar = (int)(it % kSets);   // which counter set this step uses
         const int cnext = (int)((it + 1) % kSets);
         if (threadIdx.x < R) s_done[threadIdx.x] = 0;
@@ -1173,6 +1190,11 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                         sn = __shfl_sync(pm, mine, (int)(threadIdx.x & 30) + 1);
                     } else {
                         sum_partials<sizeof(X) == 4>(p, r, i, ss, sn, sc.ppar);
+                    }
+                    if (offs) {   // the products of D = x + dref
+                        const double dr = p.dref[(it & 1) * R + r];
+                        ss = fma(dr, p.rowsum_e[i], ss);
+                        sn = fma(dr, p.rowsum_n[i], sn);
                     }
                     if (writer) {
                         p.tld[q] = -ss;   // ELSM * (0 - DispOld)
@@ -1227,7 +1249,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                     else if (o.Instab == 4) QDFN_CUR(sw, sw_n)[q] = 0;
                 }
                 Vnew = o.V;
-                if constexpr (!HM) reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)o.Disp;
+                if constexpr (!HM) {
+                    const double d0 = offs ? QDFN_CUR(D, Dn)[(int64_t)r * N] : 0.0;
+                    reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)(o.Disp - d0);
+                }
             } else {
                 if (!writer) return;   // loading faults (Solvers :370-377)
                 if (p.sw_used) p.sw_used[q] = 2;
@@ -1239,7 +1264,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 p.instab[q] = 0; p.flag[q] = 1;
                 red_min(r, 1, Dt);
                 Vnew = Vc;
-                if constexpr (!HM) reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)Dn;
+                if constexpr (!HM) {
+                    const double d0 = offs ? QDFN_CUR(D, Dn)[(int64_t)r * N] : 0.0;
+                    reinterpret_cast<X*>(p.xd)[(size_t)(par ^ 1) * p.xd_stride + i * R + r] = (X)(Dn - d0);
+                }
             }
             if constexpr (!HM) fence_proxy_async_global();
             // the next step's Accel, solver switch and time-control statistics
@@ -1725,7 +1753,8 @@ __global__ void k_fill_xd(SimParams p) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (int64_t)R * p.N) return;
     const int r = (int)(q / p.N);
-    reinterpret_cast<X*>(p.xd)[(q - (int64_t)r * p.N) * R + r] = (X)p.D[q];
+    const double d0 = (sizeof(X) == 4 && p.rowsum_e) ? p.D[(int64_t)r * p.N] : 0.0;
+    reinterpret_cast<X*>(p.xd)[(q - (int64_t)r * p.N) * R + r] = (X)(p.D[q] - d0);
 }
 
 // Operator-only kernel (qdfn_apply_operator): one pass of P2 + chunk reduction.
@@ -1771,6 +1800,11 @@ __global__ void k_chunk_reduce(SimParams p) {
     const int64_t i = q - (int64_t)r * p.N;
     double ss, sn;
     sum_partials<kPairs>(p, r, i, ss, sn);
+    if (kPairs && p.rowsum_e) {   // D = x + D(patch 0), as k_fill_xd wrote x
+        const double d0 = p.D[(int64_t)r * p.N];
+        ss = fma(d0, p.rowsum_e[i], ss);
+        sn = fma(d0, p.rowsum_n[i], sn);
+    }
     p.tld[q] = -ss;
     p.knd[q] = sn;
 }
@@ -1815,6 +1849,31 @@ __global__ void k_convert(const double* __restrict__ Ks, const double* __restric
             reinterpret_cast<uint32_t*>(Kn)[o] = split(k);
         }
     }
+}
+
+// Row sums of the stored FP32 / BF16 hi+lo operator in FP64 (the values the
+// products multiply, decoded as the operator warps decode them): one thread
+// per receiver row, stepping over the source columns of its row block
+// (consecutive rows are consecutive words).
+__global__ void k_rowsum(int64_t N, int64_t rpb, int prec, const void* E, const void* Kn, double* rse,
+                         double* rsn) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int64_t base = (i / rpb) * N * rpb + i % rpb;
+    double se = 0.0, sn = 0.0;
+    for (int64_t j = 0; j < N; ++j) {
+        const int64_t o = base + j * rpb;
+        if (prec == QDFN_FP32) {
+            se += (double)reinterpret_cast<const float*>(E)[o];
+            sn += (double)reinterpret_cast<const float*>(Kn)[o];
+        } else {
+            const uint32_t a = reinterpret_cast<const uint32_t*>(E)[o], b = reinterpret_cast<const uint32_t*>(Kn)[o];
+            se += (double)(__uint_as_float(a & 0xFFFF0000u) + __uint_as_float(a << 16));
+            sn += (double)(__uint_as_float(b & 0xFFFF0000u) + __uint_as_float(b << 16));
+        }
+    }
+    rse[i] = se;
+    rsn[i] = sn;
 }
 
 }  // namespace
