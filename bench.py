@@ -63,6 +63,8 @@ def parse():
                     help="ensemble (default, C4): 64 fault networks of 800-6,000 patches x 4 friction draws in "
                          "one persistent launch; network (C2): the 30-fault network x 4 draws")
     ap.add_argument("--geometries", type=int, default=64)
+    ap.add_argument("--tri-edge", type=float, default=80.0,
+                    help="tri_h: triangle edge in m (80: ~50,000 triangles; 160: ~12,500)")
     ap.add_argument("--cpu-members", type=int, default=4,
                     help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
     ap.add_argument("--rebalance-every", type=int, default=100,
@@ -1005,7 +1007,7 @@ def run_tri_h(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
-    net = synth.curved_fault_network(seed=args.seed)
+    net = synth.curved_fault_network(seed=args.seed, edge=args.tri_edge)
     seg = net["seg"]
     P1, P2, P3, un, _, _, us = geometry.rot_verts_unit_vectors_abi(seg, seg[:, 9])
     cen = (P1 + P2 + P3) / 3
@@ -1034,6 +1036,7 @@ def run_tri_h(args):
     def timed(sim):
         sim.run(args.warmup, timeout_s=TIMEOUT)
         T0 = sim.state(0)["T"]
+        c0 = sim.counters()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -1042,19 +1045,22 @@ def run_tri_h(args):
         torch.cuda.synchronize()
         sim.sync()
         ms = e0.elapsed_time(e1)
-        return ms, (sim.state(0)["T"] - T0) / YEAR
+        c1 = sim.counters()
+        ph = {k: (c1[k] - c0[k]) / 1e6 / args.steps for k in ("ns_control", "ns_operator", "ns_solve", "ns_rotate")}
+        ph["solve_passes_per_step"] = (c1["solve_passes"] - c0["solve_passes"]) / args.steps
+        return ms, (sim.state(0)["T"] - T0) / YEAR, ph
 
     sim = make(prec)
     clocks = ClockSampler(0)
     clocks.start()
     time.sleep(0.3)
-    ms, yrs = timed(sim)
+    ms, yrs, phases = timed(sim)
     clk = clocks.stop()
     sim.close()
     fp64 = None
     if not args.no_fp64 and prec != "fp64":
         s64 = make("fp64")
-        ms64, yrs64 = timed(s64)
+        ms64, yrs64, _ = timed(s64)
         s64.close()
         fp64 = {"value": yrs64 / (ms64 / 1e3 / 3600.0), "ms_per_step": ms64 / args.steps,
                 "mixed_over_fp64": (yrs / ms) / (yrs64 / ms64)}
@@ -1067,8 +1073,8 @@ def run_tri_h(args):
             "unit": "sim-years/hour", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "%s-operator/fp64-state" % prec, "data": "synthetic (seeded curved fault meshes)",
-            "config": {"workload": "C3: 5 curved faults, %d triangles (TDstressHS), H-matrix leaf 64, eta 2, ACA 1e-6, "
-                                   "blocks %s" % (N, prec),
+            "config": {"workload": "C3: 5 curved faults, %d triangles (TDstressHS, edge %g m), H-matrix leaf 64, "
+                                   "eta 2, ACA 1e-6, blocks %s" % (N, args.tri_edge, prec),
                        "patches": N, "blocks": int(H.nblocks), "low_rank_blocks": nlr,
                        "max_rank": int(max(ranks)) if ranks else 0, "mean_rank": float(np.mean(ranks)) if ranks else 0,
                        "stored_entries": int(stored), "compression_vs_dense": float(stored / (2.0 * N * N)),
@@ -1078,7 +1084,8 @@ def run_tri_h(args):
                          "traffic": None,
                          "note": "k_sim<H> persistent kernel, algorithmic bytes = K x stored block bytes "
                                  "(%d entries x %d B); peak %s" % (stored, esz, peak_kind)},
-            "fp64_gpu": fp64, "clocks": clk}
+            "fp64_gpu": fp64, "clocks": clk,
+            "phases_ms_per_step": {k.replace("ns_", ""): v for k, v in phases.items()}}
     print(json.dumps(line))
 
 

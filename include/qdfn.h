@@ -200,6 +200,17 @@ int qdfn_kernels_per_run(const qdfn_ctx* ctx);
 int qdfn_set_blocks(qdfn_ctx* ctx, int nblocks);
 int qdfn_get_blocks(const qdfn_ctx* ctx);
 
+/* Dense FP32/BF16 operator: column chunks of the NEXT step that a step's
+ * operator warps stream during its own solve tail (0..64; default 64, i.e. as
+ * many as are ready).  0 turns the early stream off: the operator warps then
+ * join the solves once their own tiles are in, which pays where a context is
+ * bound by its FP64 patch solves rather than by its operator stream (small
+ * ensemble members).  Results are bit-identical for every value; only the
+ * schedule changes.  qdfn_get_early_cols returns the setting (-1 for a null
+ * context).  No counterpart in the reference. */
+int qdfn_set_early_cols(qdfn_ctx* ctx, int cols);
+int qdfn_get_early_cols(const qdfn_ctx* ctx);
+
 /* ---- ensembles: many contexts in one persistent launch ------------------- */
 /* Batched ensembles of fault networks of uneven size (no counterpart in the
  * reference, which runs one geometry per Julia process; each member is the

@@ -11,8 +11,9 @@
 // handed out in a fixed order over every warp of the grid (tree leaves hold at
 // most `leaf` patches, so near-field blocks are small and a block per CTA
 // would leave most threads idle):
-//   A: t_b[kk] = Vt_b[kk,:] x[src]    one task per (low-rank block, rank row):
-//                                     lanes stride the row, coalesced, warp sum
+//   A: t_b[kk] = Vt_b[kk,:] x[src]    one task per (low-rank block, group of
+//                                     rank rows): lanes stride the rows,
+//                                     coalesced, warp sums
 //   B: partial(b, i) = (D_b x[src])_i or (U_b t_b)_i
 //                                     one task per (block, 64-row slice): a
 //                                     lane per row (two rows), the x or t
@@ -20,14 +21,14 @@
 //                                     by shuffles, coalesced loads of D^T / U^T
 // and every receiver row then sums its partials in block order (a fixed
 // order, so results are reproducible run to run).  Tasks are listed largest
-// first, so the static round-robin spreads the long ones over the warps.
+// first and dealt out to the warps in snake order, which spreads the long ones.
 #pragma once
 #include "qdfn_internal.h"
 
 namespace qdfn {
 namespace hmat {
 
-struct Blk {
+struct Blk {   // 72 bytes
     int64_t s0, ns, r0, nr;
     int64_t off_a;   // dense: D^T offset; low-rank: Vt offset
     int64_t off_b;   // low-rank: U^T offset
@@ -41,7 +42,7 @@ struct Ops {
     const Blk* blk;          // [2][nb]: shear blocks then normal blocks
     int64_t nb;
     const void* store;       // element storage
-    const int64_t* lr_list;  // pass-A tasks: (blk index << 8) | rank row
+    const int64_t* lr_list;  // pass-A tasks: (blk index << 8) | first rank row of the group
     int64_t n_lr;
     const int64_t* tile_list;   // pass-B tasks: (blk index << 20) | 64-row slice
     int64_t n_tiles;
@@ -51,6 +52,8 @@ struct Ops {
     const int64_t* rowslot;  // slot indices
 };
 
+static_assert(sizeof(Blk) == 72 && alignof(Blk) == 8, "Blk is read as nine 8-byte words");
+
 constexpr int kSliceRows = 64;     // pass-B rows per warp task (two per lane)
 constexpr int kChunk = 1024;       // (shared-memory sizing of the H launches)
 constexpr int kMaxRank = 128;
@@ -59,63 +62,170 @@ __device__ __forceinline__ int64_t warp_id_global() {
     return (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
 }
 __device__ __forceinline__ int64_t warps_global() { return (int64_t)gridDim.x * (blockDim.x >> 5); }
+// Task k of warp w among W warps: the lists are sorted largest first and dealt
+// out in snake order (rounds alternate direction), so that no warp takes the
+// largest task of every round
+__device__ __forceinline__ int64_t snake_task(int64_t k, int64_t w, int64_t W) {
+    return k * W + ((k & 1) ? W - 1 - w : w);
+}
 
-// pass A: t_b = Vt_b x[src]
-template <class T, int R>
-__device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*, double*) {
-    const int lane = threadIdx.x & 31;
-    const T* st = reinterpret_cast<const T*>(h.store);
-    for (int64_t q = warp_id_global(); q < h.n_lr; q += warps_global()) {
-        const int64_t code = h.lr_list[q];
-        const Blk b = h.blk[code >> 8];
-        const int kk = (int)(code & 255);
-        const T* row = st + b.off_a + (int64_t)kk * b.ns;
-        // each lane's products summed in T -- FP32 storage as an error-free
-        // (hi, lo) pair on the FP32 pipe -- then the warp's sum in FP64
-        T hi[R], lo[R];
+// rank rows per pass-A task: each lane keeps (hi, lo) sums for every row and
+// instance in registers
+template <int R>
+__host__ __device__ constexpr int rows_a() { return R <= 2 ? 8 : 4; }
+
+// A task's block descriptor, loaded once per task: nine independent 8-byte
+// loads (every lane the same words; the array's 72-byte stride keeps only
+// 8-byte alignment)
+__device__ __forceinline__ Blk load_blk(const Blk* p) {
+    const long long* w = reinterpret_cast<const long long*>(p);
+    Blk b;
+    b.s0 = __ldg(w); b.ns = __ldg(w + 1); b.r0 = __ldg(w + 2); b.nr = __ldg(w + 3);
+    b.off_a = __ldg(w + 4); b.off_b = __ldg(w + 5); b.toff = __ldg(w + 6); b.slot = __ldg(w + 7);
+    const int2 rk = __ldg(reinterpret_cast<const int2*>(w + 8));
+    b.rank = rk.x;
+    b.pad = rk.y;
+    return b;
+}
+
+// Warp sums of G values per lane (G = 4 or 8; R instances each) kept as FP32
+// (hi, lo) pairs (FP64 storage: hi alone).  The first log2(G) butterfly levels
+// halve the values a lane holds -- at offset o a lane keeps the half its lane
+// bit o selects and adds its partner's copy of that half -- so that lane L
+// ends with the sum of value L / (32 / G) over its 32 / G-lane group; the last
+// levels are plain butterflies.  Each combine is an error-free FP32 two-sum
+// (hi) with the low parts added, so the warp reduction costs a few FP32
+// operations per value instead of a chain of FP64 additions (the FP64 pipe is
+// the GPU's narrowest).  Returns the FP64 sums in out (valid on the lanes
+// L % (32 / G) == 0); fixed order, so results are reproducible.
+template <class T, int G, int R>
+__device__ __forceinline__ void warp_sums(T (&hi)[G][R], T (&lo)[G][R], int lane, double (&out)[R]) {
+    static_assert(G == 4 || G == 8, "rank rows per task");
+    auto combine = [](T& ah, T& al, T bh, T bl) {
+        if constexpr (sizeof(T) == 4) {
+            const T s = ah + bh, bp = s - ah;
+            const T e = (ah - (s - bp)) + (bh - bp);
+            al = al + bl + e;
+            ah = s;
+        } else {
+            ah = ah + bh;
+        }
+    };
 #pragma unroll
-        for (int r = 0; r < R; ++r) { hi[r] = 0; lo[r] = 0; }
-        for (int64_t j = lane; j < b.ns; j += 32) {
-            const T v = __ldg(row + j);
+    for (int n = G, o = 16; n > 1; n >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < n / 2; ++k)
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const T p = v * (T)__ldcg(D + (int64_t)r * N + b.s0 + j);
-                if constexpr (sizeof(T) == 4) {
-                    const T sum = hi[r] + p, bp = sum - hi[r];
-                    lo[r] += (hi[r] - (sum - bp)) + (p - bp);
-                    hi[r] = sum;
-                } else {
-                    hi[r] += p;
-                }
+                const T kh = up ? hi[k + n / 2][r] : hi[k][r], sh = up ? hi[k][r] : hi[k + n / 2][r];
+                const T kl = up ? lo[k + n / 2][r] : lo[k][r], sl = up ? lo[k][r] : lo[k + n / 2][r];
+                const T oh = __shfl_xor_sync(0xffffffffu, sh, o);
+                T ol = 0;
+                if constexpr (sizeof(T) == 4) ol = __shfl_xor_sync(0xffffffffu, sl, o);
+                hi[k][r] = kh;
+                lo[k][r] = kl;
+                combine(hi[k][r], lo[k][r], oh, ol);
             }
-        }
-        double s[R];
+    }
 #pragma unroll
-        for (int r = 0; r < R; ++r) s[r] = (double)hi[r] + (double)lo[r];
+    for (int o = 16 / G; o > 0; o >>= 1)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s[r] += __shfl_xor_sync(0xffffffffu, s[r], o);
+            const T oh = __shfl_xor_sync(0xffffffffu, hi[0][r], o);
+            T ol = 0;
+            if constexpr (sizeof(T) == 4) ol = __shfl_xor_sync(0xffffffffu, lo[0][r], o);
+            combine(hi[0][r], lo[0][r], oh, ol);
         }
-        if (lane < R) {
-            double v = s[0];
 #pragma unroll
-            for (int r = 1; r < R; ++r)
-                if (lane == r) v = s[r];
-            h.t[(b.toff + kk) * R + lane] = v;
+    for (int r = 0; r < R; ++r) out[r] = sizeof(T) == 4 ? (double)hi[0][r] + (double)lo[0][r] : (double)hi[0][r];
+}
+
+// pass A: t_b = Vt_b x[src], one task per (low-rank block, group of up to
+// rows_a rank rows): the lanes stride the block's source range, each load of
+// x serving every row of the group, and each round issues the group's rows x 2
+// column loads before any of them is used (HBM latency is hidden by the loads
+// in flight, not by occupancy: one 16-warp CTA per SM)
+template <class T, int R>
+__device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*, double*) {
+    constexpr int G = rows_a<R>();
+    const int lane = threadIdx.x & 31;
+    const T* st = reinterpret_cast<const T*>(h.store);
+    const int64_t W = warps_global(), w = warp_id_global();
+    int64_t k = 0, q = snake_task(0, w, W);
+    int64_t code = q < h.n_lr ? __ldg(h.lr_list + q) : 0;
+    while (q < h.n_lr) {
+        const Blk b = load_blk(h.blk + (code >> 8));
+        const int kk0 = (int)(code & 255);
+        const int64_t qn = snake_task(++k, w, W);
+        const int64_t code_n = qn < h.n_lr ? __ldg(h.lr_list + qn) : 0;   // the next task's code, early
+        const int nrow = min(G, b.rank - kk0);
+        const T* row0 = st + b.off_a + (int64_t)kk0 * b.ns;
+        const double* xs = D + b.s0;
+        // each lane's products summed in T -- FP32 storage as an error-free
+        // (hi, lo) pair on the FP32 pipe -- then the warp's sums (warp_sums)
+        T hi[G][R], lo[G][R];
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+            for (int r = 0; r < R; ++r) { hi[g][r] = 0; lo[g][r] = 0; }
+        for (int64_t j0 = 0; j0 < b.ns; j0 += 64) {
+            T v[2][G], xv[2][R];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t j = j0 + u * 32 + lane;
+                const bool ok = j < b.ns;
+#pragma unroll
+                for (int g = 0; g < G; ++g) v[u][g] = (ok && g < nrow) ? __ldg(row0 + (int64_t)g * b.ns + j) : (T)0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) xv[u][r] = ok ? (T)__ldcg(xs + (int64_t)r * N + j) : (T)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const T pr = v[u][g] * xv[u][r];
+                        if constexpr (sizeof(T) == 4) {
+                            const T sum = hi[g][r] + pr, bp = sum - hi[g][r];
+                            lo[g][r] += (hi[g][r] - (sum - bp)) + (pr - bp);
+                            hi[g][r] = sum;
+                        } else {
+                            hi[g][r] += pr;
+                        }
+                    }
         }
+        double tot[R];
+        warp_sums<T, G, R>(hi, lo, lane, tot);
+        constexpr int kSpan = 32 / G;   // lanes per row after the halving levels
+        const int g = lane / kSpan;
+        if (lane % kSpan == 0 && g < nrow) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) h.t[(b.toff + kk0 + g) * R + r] = tot[r];
+        }
+        q = qn;
+        code = code_n;
     }
 }
 
 // pass B: per receiver-row partials of every block, 64-row slices per warp
+// (a lane per two rows).  The inner values (x of the block's sources, or t)
+// are held by the lanes and broadcast by shuffles; the matrix columns are
+// loaded eight at a time before they are used
 template <class T, int R>
 __device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*) {
+    constexpr int U = 8;
     const int lane = threadIdx.x & 31;
     const T* st = reinterpret_cast<const T*>(h.store);
-    for (int64_t q = warp_id_global(); q < h.n_tiles; q += warps_global()) {
-        const int64_t code = h.tile_list[q];
-        const Blk b = h.blk[code >> 20];
+    const int64_t W = warps_global(), w = warp_id_global();
+    int64_t k = 0, q = snake_task(0, w, W);
+    int64_t code = q < h.n_tiles ? __ldg(h.tile_list + q) : 0;
+    while (q < h.n_tiles) {
+        const Blk b = load_blk(h.blk + (code >> 20));
         const int64_t i0 = (code & ((1 << 20) - 1)) * kSliceRows;
+        const int64_t qn = snake_task(++k, w, W);
+        const int64_t code_n = qn < h.n_tiles ? __ldg(h.tile_list + qn) : 0;
         const int64_t ia = i0 + lane, ib = i0 + 32 + lane;
         const bool va = ia < b.nr, vb = ib < b.nr;
         T sa[R], sb[R];
@@ -124,7 +234,6 @@ __device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*
         const int64_t K = b.rank < 0 ? b.ns : b.rank;   // the inner dimension
         const T* base = st + (b.rank < 0 ? b.off_a : b.off_b);
         for (int64_t j0 = 0; j0 < K; j0 += 32) {
-            // the lanes hold 32 inner values (x of the block's sources, or t)
             T xv[R];
             const int64_t jl = j0 + lane;
 #pragma unroll
@@ -135,15 +244,23 @@ __device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*
                 xv[r] = (T)v;
             }
             const int L = (int)min((int64_t)32, K - j0);
-            for (int jj = 0; jj < L; ++jj) {
-                const T* col = base + (j0 + jj) * b.nr;
-                const T ma = va ? __ldg(col + ia) : (T)0;
-                const T mb = vb ? __ldg(col + ib) : (T)0;
+            for (int jb = 0; jb < L; jb += U) {
+                T ma[U], mb[U];
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const T x = __shfl_sync(0xffffffffu, xv[r], jj);
-                    sa[r] = fma(ma, x, sa[r]);
-                    sb[r] = fma(mb, x, sb[r]);
+                for (int u = 0; u < U; ++u) {
+                    const bool ok = jb + u < L;
+                    const T* col = base + (j0 + jb + u) * b.nr;
+                    ma[u] = (ok && va) ? __ldg(col + ia) : (T)0;
+                    mb[u] = (ok && vb) ? __ldg(col + ib) : (T)0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const T x = __shfl_sync(0xffffffffu, xv[r], (jb + u) & 31);
+                        sa[r] = fma(ma[u], x, sa[r]);
+                        sb[r] = fma(mb[u], x, sb[r]);
+                    }
                 }
             }
         }
@@ -153,15 +270,31 @@ __device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*
         if (vb)
 #pragma unroll
             for (int r = 0; r < R; ++r) h.part[(b.slot + ib) * R + r] = (double)sb[r];
+        q = qn;
+        code = code_n;
     }
 }
 
-// sum of the partials of receiver row i (side 0 shear, 1 normal), block order
+// sum of the partials of receiver row i (side 0 shear, 1 normal), block order;
+// eight slot indices and then eight partials are loaded before they are added
+// (in the same order), so a row's loads overlap instead of forming a chain
 template <int R>
 __device__ __forceinline__ double row_sum(const Ops& h, int side, int64_t N, int64_t i, int r) {
     const int64_t* rp = h.rowptr + side * (N + 1);
+    const int64_t q1 = __ldg(rp + i + 1);
+    int64_t q = __ldg(rp + i);
     double s = 0.0;
-    for (int64_t q = rp[i]; q < rp[i + 1]; ++q) s += __ldcg(h.part + h.rowslot[q] * R + r);
+    for (; q + 8 <= q1; q += 8) {
+        int64_t sl[8];
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) sl[u] = __ldg(h.rowslot + q + u);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(h.part + sl[u] * R + r);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; q < q1; ++q) s += __ldcg(h.part + __ldg(h.rowslot + q) * R + r);
     return s;
 }
 

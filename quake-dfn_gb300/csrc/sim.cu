@@ -911,6 +911,16 @@ extern "C" int qdfn_set_blocks(qdfn_ctx* c, int nblocks) {
 
 extern "C" int qdfn_get_blocks(const qdfn_ctx* c) { return c ? c->nblocks : -1; }
 
+extern "C" int qdfn_set_early_cols(qdfn_ctx* c, int cols) {
+    if (!c) return fail(QDFN_ERR_INVALID, "null context");
+    if (cols < 0 || cols > 64) return fail(QDFN_ERR_INVALID, "early columns must be in 0..64");
+    if (c->running) return fail(QDFN_ERR_STATE, "a run is in flight");
+    c->c_spec = cols;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_get_early_cols(const qdfn_ctx* c) { return c ? c->c_spec : -1; }
+
 // ===========================================================================
 // Ensembles: several contexts advanced by one cooperative launch
 //
@@ -1583,14 +1593,15 @@ extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, c
         // normal rows index rowslot from base_n: shift the normal CSR
         for (int64_t i = 0; i <= N; ++i) rowptr[(N + 1) + i] += base_n;
     }
-    // warp tasks, largest first: pass A one per (low-rank block, rank row)
-    // (cost ns), pass B one per (block, 64-row slice) (cost rows x inner size;
-    // a rank-0 block's task writes zero partials)
+    // warp tasks, largest first: pass A one per (low-rank block, group of
+    // rows_a rank rows) (cost ns x rows), pass B one per (block, 64-row slice)
+    // (cost rows x inner size; a rank-0 block's task writes zero partials)
+    const int ga = Rk <= 2 ? hmat::rows_a<1>() : hmat::rows_a<4>();
     std::vector<std::pair<int64_t, int64_t>> ta, tb;   // (cost, code)
     for (int64_t q = 0; q < 2 * nb; ++q) {
         const hmat::Blk& B = blk[q];
-        if (B.rank > 0)
-            for (int64_t kk = 0; kk < B.rank; ++kk) ta.push_back({B.ns, (q << 8) | kk});
+        for (int64_t kk = 0; kk < B.rank; kk += ga)
+            ta.push_back({B.ns * std::min<int64_t>(ga, B.rank - kk), (q << 8) | kk});
         const int64_t inner = B.rank < 0 ? B.ns : B.rank;
         const int64_t nt = (B.nr + hmat::kSliceRows - 1) / hmat::kSliceRows;
         for (int64_t t = 0; t < nt; ++t)

@@ -35,7 +35,7 @@ EXPORTS = [
     "qdfn_ensemble_create", "qdfn_ensemble_destroy", "qdfn_ensemble_get_blocks", "qdfn_ensemble_set_blocks",
     "qdfn_ensemble_balance", "qdfn_ensemble_run", "qdfn_ensemble_run_async", "qdfn_ensemble_sync",
     "qdfn_ensemble_shares", "qdfn_ensemble_set_fill", "qdfn_check_division", "qdfn_adjoint_run",
-    "qdfn_assemble_tri_pairs_dev",
+    "qdfn_assemble_tri_pairs_dev", "qdfn_set_early_cols", "qdfn_get_early_cols",
 ]
 
 
@@ -104,6 +104,8 @@ def load():
     L.qdfn_kernels_per_run.argtypes = [C.c_void_p]
     L.qdfn_set_blocks.argtypes = [C.c_void_p, C.c_int]
     L.qdfn_get_blocks.argtypes = [C.c_void_p]
+    L.qdfn_set_early_cols.argtypes = [C.c_void_p, C.c_int]
+    L.qdfn_get_early_cols.argtypes = [C.c_void_p]
     L.qdfn_get_counters.argtypes = [C.c_void_p, _ip, C.c_int]
     L.qdfn_get_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 8 + [_ip]
     L.qdfn_set_state.argtypes = [C.c_void_p, C.c_int] + [_dp] * 6 + [C.c_double, C.c_double, C.c_int64]

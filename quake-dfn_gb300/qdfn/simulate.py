@@ -136,6 +136,14 @@ class Simulation:
     def blocks(self):
         return self.L.qdfn_get_blocks(self._h)
 
+    def set_early_cols(self, cols):
+        """Next-step column chunks streamed in a step's solve tail (0..64; 0:
+        the operator warps join the solves instead).  Schedule only."""
+        _lib.check(self.L.qdfn_set_early_cols(self._h, int(cols)))
+
+    def early_cols(self):
+        return self.L.qdfn_get_early_cols(self._h)
+
     def counters(self):
         """Cumulative device counters: ns in time control / operator / solves /
         rotation, solve passes, steps, low-/high-velocity patch solves and their
