@@ -67,7 +67,10 @@ def parse():
                     help="tri_h: triangle edge in m (80: ~50,000 triangles; 160: ~12,500)")
     ap.add_argument("--cpu-members", type=int, default=4,
                     help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
-    ap.add_argument("--rebalance-every", type=int, default=100,
+    ap.add_argument("--plain-members", type=int, default=16,
+                    help="ensemble members (at size quantiles, one draw each) run through the plain FP64 GPU path, "
+                         "one instance per launch (0: skip)")
+    ap.add_argument("--rebalance-every", type=int, default=15,
                     help="ensemble: steps per launch in the timed window, the SMs re-divided between launches "
                          "(0: one launch)")
     ap.add_argument("--no-fill", dest="fill", action="store_false",
@@ -669,6 +672,49 @@ def ensemble_cpu_sample(args, info, hostK, start, budget_s):
             "wall_s": wall}
 
 
+def plain_fp64_sample(args, info, plainK, start, ens, stream):
+    """The plain FP64 GPU path -- the drop-in `main` as a user runs it, one
+    instance per context and launch, FP64 operator, every SM -- on one draw of
+    each sampled member (draw g mod R of member g), each from its state at the
+    timed window's start over the same K steps.  The sample spans the members'
+    size quantiles, so the ensemble's plain-path rate is estimated as the
+    sample's summed simulated years over its summed device time."""
+    import torch
+    from qdfn import simulate
+    yrs, ms_tot, rows = 0.0, 0.0, []
+    for g, (Ks, Kn) in plainK.items():
+        N = info[g]["N"]
+        r = g % args.inst
+        p = problem(info[g]["sysd"], {k: v[r * N:(r + 1) * N] for k, v in info[g]["draws"].items()},
+                    info[g]["kdiag"], 1)
+        sim = simulate.Simulation(p)
+        sim.set_dense_device(Ks, Kn, "fp64", layout="col")
+        ext = info[g]["ext"]
+        sim.set_external_stress(ext["t"], ext["normal"], ext["shear"], ext["pressure"])
+        st = start[g][r]
+        sim.set_state(0, st)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.run_async(args.steps, stream=stream.cuda_stream, timeout_s=TIMEOUT)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sim.sync()
+        ms = e0.elapsed_time(e1)
+        y = (sim.state(0)["T"] - st["T"]) / YEAR
+        ym = (ens.members[g].state(r)["T"] - st["T"]) / YEAR   # the mixed ensemble's run of the same instance
+        sim.close()
+        yrs += y
+        ms_tot += ms
+        rows.append({"member": g, "patches": N, "draw": r, "ms_per_step": ms / args.steps, "sim_years": y,
+                     "mixed_sim_years": ym})
+    return {"value": yrs / (ms_tot / 1e3 / 3600.0), "unit": "sim-years/hour", "instances_sampled": len(rows),
+            "method": "one draw of each of %d members at size quantiles, each alone on the GPU (FP64 operator, "
+                      "one instance per launch) over the timed window's K steps; rate = summed simulated years "
+                      "over summed device time" % len(rows),
+            "samples": rows}
+
+
 def run_ensemble(args):
     """C4, the headline: 64 fault networks of uneven size x 4 friction draws
     (256 instances) advanced by ONE persistent launch (qdfn_ensemble_*),
@@ -695,6 +741,8 @@ def run_ensemble(args):
             hostK[g] = (members[g]["Ks"].cpu().numpy().T, members[g]["Kn"].cpu().numpy().T)
     ens = ensemble.Ensemble(members, precision=args.precision)
     ens64 = None if args.no_fp64 else ensemble.Ensemble(members, precision="fp64")
+    plain_sample = [] if (args.no_fp64 or args.plain_members <= 0) else _member_sample(sizes, args.plain_members)
+    plainK = {g: (members[g]["Ks"], members[g]["Kn"]) for g in plain_sample}
     del members
     torch.cuda.empty_cache()
     s0 = _snapshot(ens)
@@ -796,6 +844,10 @@ def run_ensemble(args):
     traffic = None
     if prof and prof.get("instances") == len(sizes) * R and prof.get("total_patches") == sum(sizes):
         traffic = float(prof["dram_bytes_per_step"]) * args.steps
+    elif prof and prof.get("traffic_over_algorithmic"):
+        # captured on a smaller ensemble of the same generator: traffic scales
+        # with the members' algorithmic bytes
+        traffic = float(prof["traffic_over_algorithmic"]) * alg_bytes
     cnt = [sim.counters() for sim in ens.members]
     solves = sum(c1["lowv_solves"] + c1["highv_solves"] - c0["lowv_solves"] - c0["highv_solves"]
                  for c0, c1 in zip(cnt0, cnt))
@@ -852,6 +904,10 @@ def run_ensemble(args):
         ens64.close()
         ens64 = None
         torch.cuda.empty_cache()
+        if plain_sample:
+            fp64["plain_path"] = plain_fp64_sample(args, info, plainK, start, ens, stream)
+            fp64["mixed_over_plain_fp64"] = value / fp64["plain_path"]["value"]
+    plainK = None
 
     # ---- e2e through the C ABI with host buffers: every step, every member's
     # state goes up from pinned host memory, one ensemble step runs (one
@@ -921,7 +977,10 @@ def run_ensemble(args):
                          "note": "k_sim_members (one launch, every member's K steps), algorithmic bytes = K x "
                                  "sum over members (2 N^2 x %d B operator + state vectors); peak %s. The small "
                                  "members are bound by their FP64 friction solves, not by HBM: %.3g patch solves "
-                                 "per second" % (esz, peak_kind, solves / max(ms / 1e3, 1e-9))},
+                                 "per second. traffic = DRAM bytes of the K-step window: the algorithmic bytes x "
+                                 "the DRAM/algorithmic ratio of the committed ncu capture of a smaller ensemble of "
+                                 "the same generator (profiles/k_sim_members_c4_fp32.md)"
+                                 % (esz, peak_kind, solves / max(ms / 1e3, 1e-9))},
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
             "fill_mode": dict(fill, note="the same window with members that have taken K steps stepping on "
@@ -1046,7 +1105,8 @@ def run_tri_h(args):
         sim.sync()
         ms = e0.elapsed_time(e1)
         c1 = sim.counters()
-        ph = {k: (c1[k] - c0[k]) / 1e6 / args.steps for k in ("ns_control", "ns_operator", "ns_solve", "ns_rotate")}
+        ph = {k: (c1[k] - c0[k]) / 1e6 / args.steps for k in ("ns_control", "ns_operator", "ns_solve", "ns_rotate",
+                                                              "ns_solve_own", "ns_solve_wait")}
         ph["solve_passes_per_step"] = (c1["solve_passes"] - c0["solve_passes"]) / args.steps
         return ms, (sim.state(0)["T"] - T0) / YEAR, ph
 
@@ -1067,6 +1127,8 @@ def run_tri_h(args):
     peak, peak_kind = measured_peaks()
     alg = args.steps * stored * esz
     achieved = alg / (ms / 1e3) / 1e9
+    prof = profiled("k_sim_hmat_c3_fp32") if prec == "fp32" else None
+    traffic = float(prof["traffic_over_algorithmic"]) * alg if prof else None
     nlr = sum(1 for U in H.U_s + H.U_n if U is not None)
     ranks = [U.shape[1] for U in H.U_s + H.U_n if U is not None]
     line = {"metric": "sim-years/hour, triangle-mesh network with H-matrix operator", "value": yrs / (ms / 1e3 / 3600.0),
@@ -1081,9 +1143,11 @@ def run_tri_h(args):
                        "h_build_s": build_s},
             "gpu_launches": 1,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None,
+                         "traffic": traffic,
                          "note": "k_sim<H> persistent kernel, algorithmic bytes = K x stored block bytes "
-                                 "(%d entries x %d B); peak %s" % (stored, esz, peak_kind)},
+                                 "(%d entries x %d B); peak %s; traffic = those bytes x the DRAM/algorithmic "
+                                 "ratio of the committed ncu capture of a 12,500-triangle mesh of the same "
+                                 "generator (profiles/k_sim_hmat_c3_fp32.md)" % (stored, esz, peak_kind)},
             "fp64_gpu": fp64, "clocks": clk,
             "phases_ms_per_step": {k.replace("ns_", ""): v for k, v in phases.items()}}
     print(json.dumps(line))

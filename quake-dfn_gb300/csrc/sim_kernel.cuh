@@ -492,6 +492,48 @@ __device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
     return rb >= p.rb_small0 ? p.nchunk2 : p.nchunk;
 }
 
+// The state and constants of one 16-row solve chunk (rows i0..i0+15 of
+// instance r, q0 = r N + i0) toward L1, issued by the claiming warp before it
+// waits for the chunk's row block: 17 arrays, the two 128-byte lines that 16
+// consecutive elements can span, one prefetch per lane and array half.  The
+// chunk's loads in solve_item then find their lines close instead of forming
+// a chain of round trips behind the partial sums.  Hints only; the addresses
+// stay inside the arrays (the last row is clamped to N - 1).
+__device__ __forceinline__ void prefetch_chunk(const SimParams& p, int par, int r, int64_t i0) {
+    const int lane = threadIdx.x & 31;
+    const int64_t N = p.N;
+    const int64_t ie = min(i0 + 15, N - 1);
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int slot = lane + 32 * t;
+        const int a = slot >> 1;
+        if (a >= 17) continue;
+        const int64_t e = (slot & 1) ? ie : i0;   // first or last element of the run
+        const int64_t q = (int64_t)r * N + e;
+        const void* ptr;
+        switch (a) {
+            case 0: ptr = (par ? p.Vn : p.V) + q; break;
+            case 1: ptr = (par ? p.Dn : p.D) + q; break;
+            case 2: ptr = (par ? p.fn : p.fric) + q; break;
+            case 3: ptr = (par ? p.thn : p.theta) + q; break;
+            case 4: ptr = (par ? p.sn : p.sig_old) + q; break;
+            case 5: ptr = p.F0 + q; break;
+            case 6: ptr = p.a + q; break;
+            case 7: ptr = p.b + q; break;
+            case 8: ptr = p.Dc + q; break;
+            case 9: ptr = p.omega + q; break;
+            case 10: ptr = p.rDc + q; break;
+            case 11: ptr = p.ra + q; break;
+            case 12: ptr = p.mass + q; break;
+            case 13: ptr = p.sigma0 + q; break;
+            case 14: ptr = p.tau0 + q; break;
+            case 15: ptr = p.kself + e; break;
+            default: ptr = (par ? p.sw_n : p.sw) + q; break;
+        }
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+    }
+}
+
 // One matrix's half of sum_partials (side 0 shear, 1 normal), for a lane pair
 // that splits the two sums between its lanes; same order and arithmetic.
 template <bool kPairs>
@@ -1175,12 +1217,17 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
 #define QDFN_NXT(a, b) (par ? p.a : p.b)
         auto solve_item = [&](int64_t q, int r, int64_t i, bool first, bool pair) {
             const bool writer = !pair || (threadIdx.x & 1) == 0;
+            // the row's products: formed here in a step's first pass (and kept
+            // in registers for this solve), read back in a retry pass
+            double tld_q = 0.0, knd_q = 0.0;
             if (first) {
                 if constexpr (HM) {
                     // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
                     const double ss = hmat::row_sum<R>(p.h, 0, N, i, r);
-                    p.tld[q] = (-ss) / -p.kself[i];
-                    p.knd[q] = hmat::row_sum<R>(p.h, 1, N, i, r);
+                    tld_q = (-ss) / -p.kself[i];
+                    knd_q = hmat::row_sum<R>(p.h, 1, N, i, r);
+                    p.tld[q] = tld_q;
+                    p.knd[q] = knd_q;
                 } else {
                     double ss, sn;
                     if (pair) {   // the even lane sums the shear partials, the odd lane the normal ones
@@ -1196,12 +1243,16 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                         ss = fma(dr, p.rowsum_e[i], ss);
                         sn = fma(dr, p.rowsum_n[i], sn);
                     }
+                    tld_q = -ss;   // ELSM * (0 - DispOld)
+                    knd_q = sn;    // StiffnessMatrixNormal * DispOld
                     if (writer) {
-                        p.tld[q] = -ss;   // ELSM * (0 - DispOld)
-                        p.knd[q] = sn;    // StiffnessMatrixNormal * DispOld
+                        p.tld[q] = tld_q;
+                        p.knd[q] = knd_q;
                     }
-                    if (pair) __syncwarp(3u << (threadIdx.x & 30));   // the odd lane reads them below
                 }
+            } else {
+                tld_q = p.tld[q];
+                knd_q = p.knd[q];
             }
             const double Dt = s_dt[r];
             double dsn = 0, dss = 0, dsp = 0;
@@ -1209,7 +1260,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 const double tq = p.interp_at_told ? s_T[r] : s_T[r] + Dt;
                 sim::interp_ext(p.n_ext, p.ext_t, p.ext_n, p.ext_s, p.ext_p, N, i, tq, dsn, dss, dsp);
             }
-            double sig = p.knd[q] + p.sigma0[q] + dsn;
+            double sig = knd_q + p.sigma0[q] + dsn;
             if (sig < p.sigma_min) sig = p.sigma_min;
             const double VOld = QDFN_CUR(V, Vn)[q];
             double Vnew;
@@ -1220,7 +1271,7 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 pin.VOld = VOld; pin.Friction0 = p.F0[q]; pin.a = p.a[q]; pin.b = p.b[q];
                 pin.Dc = p.Dc[q]; pin.K_Self = p.kself[i]; pin.Omega = p.omega[q];
                 pin.rDc = p.rDc[q]; pin.ra = p.ra[q]; pin.rDt = s_rdt[r];
-                pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + p.tld[q];
+                pin.Mass = p.mass[q]; pin.sigma = sig; pin.TLD = 0.0 + tld_q;
                 pin.dtau = dss; pin.sigma_old = QDFN_CUR(sig_old, sn)[q]; pin.tau0 = p.tau0[q];
                 int err = 0;
                 sim::PatchOut o;
@@ -1397,7 +1448,9 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                     const int64_t rbp = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
                     const int64_t rb = sc.order ? (int64_t)sc.order[rbp] : rbp;   // in the step's order
                     const int r = (int)(rem / cpr);
-                    const int64_t i = rb * rpb + (rem % cpr) * 16 + (lane >> 1);
+                    const int64_t i0 = rb * rpb + (rem % cpr) * 16;
+                    const int64_t i = i0 + (lane >> 1);
+                    if (i0 < N) prefetch_chunk(p, par, r, i0);
                     int ok = 1;
                     if (lane == 0) {   // bounded wait for the row block's last column chunk
                         const unsigned need = (unsigned)chunks_of_rb(p, rb) * kOpWarps;   // one per warp and tile

@@ -9,7 +9,8 @@ pair (QDFN_PAIR_SOLVE=1) or on one lane.  None of this may change a result: ever
 summed over the same column chunks in the same order, and the lane-pair solver
 performs the one-lane solver's arithmetic.  So runs that differ only in these
 settings must agree bit for bit -- through a loaded network that reaches the
-high-velocity solver and retried steps.
+high-velocity solver and retried steps.  The per-context early-column setting
+(qdfn_set_early_cols) is a schedule setting like the others.
 """
 import os
 
@@ -37,9 +38,10 @@ def loaded_network(qdfn_mod):
     return prob, Ks, Kn, ext
 
 
-def _run(net, env, nsteps, chunk, precision):
+def _run(net, env, nsteps, chunk, precision, early=None):
     """States after every `chunk` steps, with `env` set while the context is
-    configured (the schedule settings are read then)."""
+    configured (the schedule settings are read then); `early`: the context's
+    early-column setting."""
     from qdfn import simulate
     prob, Ks, Kn, ext = net
     old = {k: os.environ.get(k) for k in env}
@@ -48,6 +50,8 @@ def _run(net, env, nsteps, chunk, precision):
         sim = simulate.Simulation(prob, n_inst=2)
         sim.set_dense(Ks, Kn, precision)
         sim.set_blocks(16)
+        if early is not None:
+            sim.set_early_cols(early)
     finally:
         for k, v in old.items():
             if v is None:
@@ -85,3 +89,12 @@ def test_early_tiles_and_lane_pairs_change_no_bit(qdfn_mod, loaded_network, prec
                 {"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 0, "QDFN_RB_ORDER": 1}):
         got, _ = _run(loaded_network, env, nsteps, chunk, precision)
         _same(ref, got)
+
+
+def test_early_columns_per_context_change_no_bit(qdfn_mod, loaded_network):
+    nsteps, chunk = 200, 100
+    ref, _ = _run(loaded_network, {}, nsteps, chunk, "fp32")
+    for cols in (0, 1, 64):
+        got, _ = _run(loaded_network, {}, nsteps, chunk, "fp32", early=cols)
+        _same(ref, got)
+
