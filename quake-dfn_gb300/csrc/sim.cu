@@ -84,7 +84,8 @@ struct qdfn_ctx {
     int64_t xbuf = 0;                // elements per shared-memory x buffer
     int64_t xd_stride = 0, rb_stride = 0;
     int hold_cap = 8;                // row chunks a block may hold at once (QDFN_SOLVE_HOLD)
-    int pair_solve = 1;              // lane-pair solves in the overlapped phase (QDFN_PAIR_SOLVE=0: one lane)
+    int pair_solve = 2;              // overlapped-phase solves: 2 one lane per patch, 32-row chunks; 1 lane
+                                     // pairs, 16-row chunks; 0 even lanes alone (QDFN_PAIR_SOLVE)
     int rb_ordered = 1;              // high-velocity row blocks first (QDFN_RB_ORDER=0: index order)
     int c_spec = 64;                 // next-step column chunks streamed in a step's tail (QDFN_SPEC_COLS;
                                      // at most the chunks of a full-width row block, so 64: all of them)
@@ -224,6 +225,7 @@ int configure_launch(qdfn_ctx* c) {
     // several contexts run side by side); the tiling is sized for them
     const int sms = c->nblocks_override > 0 ? std::min(dev_sms, c->nblocks_override) : dev_sms;
     SimKernel k = sim_kernel(c->prec, c->R, c->hmat != 0);
+    if (const char* e = std::getenv("QDFN_PAIR_SOLVE")) c->pair_solve = std::max(0, std::min(2, std::atoi(e)));
     int64_t want_blocks;
     if (c->hmat) {
         c->smem = (size_t)Rk * hmat::kChunk * xsz + (size_t)hmat::kMaxRank * Rk * sizeof(double);
@@ -239,7 +241,6 @@ int configure_launch(qdfn_ctx* c) {
         int64_t tiles_per_sm = 4;
         if (const char* e = std::getenv("QDFN_TILES_PER_SM")) tiles_per_sm = std::max(1, std::min(64, std::atoi(e)));
         if (const char* e = std::getenv("QDFN_SOLVE_HOLD")) c->hold_cap = std::max(1, std::min(64, std::atoi(e)));
-        if (const char* e = std::getenv("QDFN_PAIR_SOLVE")) c->pair_solve = std::atoi(e) != 0 ? 1 : 0;
         if (const char* e = std::getenv("QDFN_RB_ORDER")) c->rb_ordered = std::atoi(e) != 0 ? 1 : 0;
         if (const char* e = std::getenv("QDFN_SPEC_COLS")) c->c_spec = std::max(0, std::min(64, std::atoi(e)));
         if (const char* e = std::getenv("QDFN_SPEC_STOP")) c->spec_stop_pct = std::max(1, std::min(100, std::atoi(e)));

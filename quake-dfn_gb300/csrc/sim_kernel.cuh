@@ -125,7 +125,8 @@ struct SimParams {
     unsigned long long* prof;       // cumulative counters (qdfn_get_counters)
     int64_t n_rb;                    // dense: operator row blocks
     int hold_cap;                    // dense: row chunks a block may hold at once in the overlapped phase
-    int pair_solve;                  // overlapped phase: one lane pair per patch (else the even lanes alone)
+    int pair_solve;                  // overlapped phase: 1 one lane pair per patch, 16-row chunks; 2 one
+                                     // lane per patch, 32-row chunks; 0 the even lanes alone, 16-row chunks
     int rb_ordered;                  // FP32/BF16 dense: row blocks with high-velocity patches first
     int c_spec;                      // dense: column chunks of the next step streamed during a step's tail
     int spec_stop;                   // no early-tile claims once this many blocks reached the step's barrier
@@ -492,23 +493,28 @@ __device__ __forceinline__ int chunks_of_rb(const SimParams& p, int64_t rb) {
     return rb >= p.rb_small0 ? p.nchunk2 : p.nchunk;
 }
 
-// The state and constants of one 16-row solve chunk (rows i0..i0+15 of
-// instance r, q0 = r N + i0) toward L1, issued by the claiming warp before it
-// waits for the chunk's row block: 17 arrays, the two 128-byte lines that 16
-// consecutive elements can span, one prefetch per lane and array half.  The
+// Rows of one solve chunk of the overlapped phase: 16 on lane pairs, 32 with
+// one lane per patch.
+__device__ __forceinline__ int solve_rows(const SimParams& p) { return p.pair_solve == 2 ? 32 : 16; }
+
+// The state and constants of one solve chunk (rows i0..i0+rows-1 of instance
+// r, rows 16 or 32) toward L1, issued by the claiming warp before it waits for
+// the chunk's row block: 17 arrays, the 128-byte lines that the run can span
+// (its first, middle and last element), one or two prefetches per lane.  The
 // chunk's loads in solve_item then find their lines close instead of forming
 // a chain of round trips behind the partial sums.  Hints only; the addresses
 // stay inside the arrays (the last row is clamped to N - 1).
-__device__ __forceinline__ void prefetch_chunk(const SimParams& p, int par, int r, int64_t i0) {
+__device__ __forceinline__ void prefetch_chunk(const SimParams& p, int par, int r, int64_t i0, int rows) {
     const int lane = threadIdx.x & 31;
     const int64_t N = p.N;
-    const int64_t ie = min(i0 + 15, N - 1);
+    const int64_t ie = min(i0 + rows - 1, N - 1);
+    const int64_t im = min(i0 + rows / 2, N - 1);
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
         const int slot = lane + 32 * t;
-        const int a = slot >> 1;
+        const int a = slot / 3, l = slot % 3;
         if (a >= 17) continue;
-        const int64_t e = (slot & 1) ? ie : i0;   // first or last element of the run
+        const int64_t e = l == 0 ? i0 : (l == 1 ? im : ie);   // first, middle or last element of the run
         const int64_t q = (int64_t)r * N + e;
         const void* ptr;
         switch (a) {
@@ -788,7 +794,7 @@ __device__ __forceinline__ bool produce_stage(const SimParams& p, Pipe& pp, type
             const long long t = rb * p.nchunk + c;
             // its x chunk: the slip of patches [j0, j0 + L), solved in this step
             const TileGeo g = tile_geo(p, nrb, t);
-            const unsigned need = (unsigned)(R * (rows_per_blk / 16));   // solve chunks per row block
+            const unsigned need = (unsigned)(R * (rows_per_blk / solve_rows(p)));   // solve chunks per row block
             const uint64_t t0 = globaltimer_ns();
             for (int64_t b = g.j0 / rows_per_blk; b <= (int64_t)(g.j0 + g.L - 1) / rows_per_blk; ++b)
                 while (ld_acquire_u32(p.rb_solved + sc.set * p.rb_stride + b) < need) {
@@ -1411,7 +1417,8 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             }
             if (solve) {
                 constexpr int64_t rpb = (int64_t)kOpThreads * M::VEC;   // operator row block
-                constexpr int64_t cpr = rpb / 16;     // 16-row chunks (one lane pair per row) per block and instance
+                const int crows = solve_rows(p);
+                const int64_t cpr = rpb / crows;     // row chunks per block and instance
                 const int64_t nk = p.n_rb * R * cpr;
                 const unsigned* rbd = p.rb_done + cpar * p.rb_stride;
                 for (;;) {
@@ -1448,9 +1455,9 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                     const int64_t rbp = (int64_t)k / (R * cpr), rem = (int64_t)k % (R * cpr);
                     const int64_t rb = sc.order ? (int64_t)sc.order[rbp] : rbp;   // in the step's order
                     const int r = (int)(rem / cpr);
-                    const int64_t i0 = rb * rpb + (rem % cpr) * 16;
-                    const int64_t i = i0 + (lane >> 1);
-                    if (i0 < N) prefetch_chunk(p, par, r, i0);
+                    const int64_t i0 = rb * rpb + (rem % cpr) * crows;
+                    const int64_t i = i0 + (crows == 32 ? lane : (lane >> 1));
+                    if (i0 < N) prefetch_chunk(p, par, r, i0, crows);
                     int ok = 1;
                     if (lane == 0) {   // bounded wait for the row block's last column chunk
                         const unsigned need = (unsigned)chunks_of_rb(p, rb) * kOpWarps;   // one per warp and tile
@@ -1472,10 +1479,12 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                         break;
                     }
                     const uint64_t t_ready = globaltimer_ns();
-                    // QDFN_PAIR_SOLVE=0: the even lane alone solves the patch with the
-                    // one-lane solver (same results; the lane-pair check uses it)
-                    if (i < N && (p.pair_solve || (lane & 1) == 0))
-                        solve_item((int64_t)r * N + i, r, i, true, p.pair_solve != 0);
+                    // pair_solve 0: the even lane alone solves the patch with the one-lane
+                    // solver (same results; the lane-pair check uses it); 2: every lane
+                    // solves its own patch with the one-lane solver -- fewer FP64
+                    // operations per patch (no duplicated secant step), longer chains
+                    if (i < N && (p.pair_solve != 0 || (lane & 1) == 0))
+                        solve_item((int64_t)r * N + i, r, i, true, p.pair_solve == 1);
                     __syncwarp();
                     if (lane == 0) {
                         atomicSub(&s_held, 1);

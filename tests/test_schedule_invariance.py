@@ -5,7 +5,8 @@ whichever SM asks next, a step streams the next step's first column chunks
 during its own solve tail (QDFN_SPEC_COLS early column chunks, discarded when
 the step retries), row blocks holding high-velocity patches go first
 (QDFN_RB_ORDER=1) or all go in index order, and each patch is solved on a lane
-pair (QDFN_PAIR_SOLVE=1) or on one lane.  None of this may change a result: every row's products are
+pair (QDFN_PAIR_SOLVE=1, 16-row chunks) or on one lane (2: every lane, 32-row
+chunks; 0: the even lanes alone).  None of this may change a result: every row's products are
 summed over the same column chunks in the same order, and the lane-pair solver
 performs the one-lane solver's arithmetic.  So runs that differ only in these
 settings must agree bit for bit -- through a loaded network that reaches the
@@ -86,7 +87,9 @@ def test_early_tiles_and_lane_pairs_change_no_bit(qdfn_mod, loaded_network, prec
     for env in ({"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 1, "QDFN_RB_ORDER": 1},     # the defaults
                 {"QDFN_SPEC_COLS": 16, "QDFN_PAIR_SOLVE": 1, "QDFN_RB_ORDER": 1},    # every column chunk early
                 {"QDFN_SPEC_COLS": 0, "QDFN_PAIR_SOLVE": 1, "QDFN_RB_ORDER": 0},
-                {"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 0, "QDFN_RB_ORDER": 1}):
+                {"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 0, "QDFN_RB_ORDER": 1},
+                {"QDFN_SPEC_COLS": 8, "QDFN_PAIR_SOLVE": 2, "QDFN_RB_ORDER": 1},     # one lane per patch, 32 rows
+                {"QDFN_SPEC_COLS": 0, "QDFN_PAIR_SOLVE": 2, "QDFN_RB_ORDER": 0}):
         got, _ = _run(loaded_network, env, nsteps, chunk, precision)
         _same(ref, got)
 
