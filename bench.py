@@ -909,43 +909,39 @@ def run_ensemble(args):
             fp64["mixed_over_plain_fp64"] = value / fp64["plain_path"]["value"]
     plainK = None
 
-    # ---- e2e through the C ABI with host buffers: every step, every member's
-    # state goes up from pinned host memory, one ensemble step runs (one
-    # launch), the state comes back; one synchronisation per step
+    # ---- e2e through the C ABI with host buffers: every step the whole
+    # ensemble's state goes up from pinned host memory in one copy
+    # (qdfn_ensemble_set_state_all), one ensemble step runs (one launch), the
+    # state comes back in one copy (qdfn_ensemble_get_state_all, which also
+    # completes the run: one synchronisation per step)
     e2e = None
     if not args.no_e2e:
         _restore(ens, start)
-        names = ensemble.simulate.Simulation.STATE_FIELDS
-        bufs = []
-        for m, sim in enumerate(ens.members):
-            blk = torch.empty((len(names), sim.n_inst, sim.N), dtype=torch.float64).pin_memory()
-            for f, k in enumerate(names):
-                blk[f].copy_(torch.from_numpy(np.stack([start[m][r][k] for r in range(sim.n_inst)])))
-            Tdt = torch.tensor([[start[m][r]["T"] for r in range(sim.n_inst)],
-                                [start[m][r]["dt"] for r in range(sim.n_inst)]], dtype=torch.float64).pin_memory()
-            stp = torch.tensor([start[m][r]["step"] for r in range(sim.n_inst)], dtype=torch.int64).pin_memory()
-            bufs.append(({k: blk[f] for f, k in enumerate(names)}, Tdt, stp))
+        buf = torch.empty(ens.state_words(), dtype=torch.float64).pin_memory()
+        ens.pack_states(start, out=buf)
         sptr = stream.cuda_stream
-        nbytes = sum(6 * sim.n_inst * sim.N * 8 + sim.n_inst * 24 for sim in ens.members)
+        nbytes = ens.state_words() * 8
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            for sim, (arr, Tdt, stp) in zip(ens.members, bufs):
-                sim.set_state_all(arr, Tdt[0], Tdt[1], stp, stream=sptr)
+        for k in range(args.steps):
+            ens.set_state_all(buf, stream=sptr)
             ens.run_async(1, timeout_s=TIMEOUT, stream=sptr)
-            for sim, (arr, Tdt, stp) in zip(ens.members, bufs):
-                sim.get_state_all(arr, Tdt[0], Tdt[1], stp, stream=sptr, wait=False)
-            ens.sync()
+            ens.get_state_all(buf, stream=sptr, wait=True)
+            if args.rebalance_every > 0 and (k + 1) % args.rebalance_every == 0 and k + 1 < args.steps:
+                ens.balance()
         t_e2e = time.perf_counter() - t0
         if ws > 1:
             t_e2e = max_over_ranks(t_e2e, dev)
-        ye = sum(float(bufs[m][1][0][r].item() - start[m][r]["T"]) for m, sim in enumerate(ens.members)
+        fin = ens.unpack_states(buf)
+        ye = sum(fin[m][r]["T"] - start[m][r]["T"] for m, sim in enumerate(ens.members)
                  for r in range(sim.n_inst)) / YEAR
         if ws > 1:
             ye = sum_over_ranks(ye, dev)
         e2e = {"value": ye / (t_e2e / 3600.0), "unit": "sim-years/hour", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes,
-               "note": "one ensemble step per launch (no step streams ahead across a launch boundary)"}
+               "note": "one ensemble step per launch, the whole state up and down every step in one copy each "
+                       "way (no step streams ahead across a launch boundary); the SMs re-divided every "
+                       "rebalance_every steps as in the device-resident window"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

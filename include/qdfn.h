@@ -255,6 +255,22 @@ int qdfn_ensemble_run(qdfn_ensemble* ens, int64_t nsteps, double timeout_s);
  * steps each (read their step counts back).  The extra steps are ordinary
  * steps of each member's own trajectory. */
 int qdfn_ensemble_set_fill(qdfn_ensemble* ens, int on);
+
+/* All members' state in ONE host<->device copy each way (an ensemble's
+ * end-to-end step: state up, one ensemble step, state down).  The host buffer
+ * (qdfn_ensemble_state_bytes bytes; pinned for asynchronous copies) holds, member
+ * after member in the order given at creation, the six fields of
+ * qdfn_set_state_all as [6][n_inst][N] doubles (V, D, theta, friction, accel,
+ * sigma_old), then T[n_inst], dt[n_inst] and step[n_inst] (int64) as 8-byte
+ * words.  set: enqueued on `stream`; no run may be in flight.  get: enqueued on
+ * `stream`; with wait = 1 it returns once the state is on the host, and if an
+ * ensemble run is in flight on the same stream it completes that run (its
+ * outcome is returned, as qdfn_ensemble_sync does).  The per-context calls
+ * qdfn_set_state_all / qdfn_get_state_all move the same data member by member;
+ * no counterpart in the reference, which runs one geometry per process. */
+int qdfn_ensemble_state_bytes(const qdfn_ensemble* ens, int64_t* bytes);
+int qdfn_ensemble_set_state_all(qdfn_ensemble* ens, const void* host, void* stream);
+int qdfn_ensemble_get_state_all(qdfn_ensemble* ens, void* host, void* stream, int wait);
 int qdfn_ensemble_run_async(qdfn_ensemble* ens, int64_t nsteps, double timeout_s, void* stream);
 int qdfn_ensemble_sync(qdfn_ensemble* ens);
 /* Host-only split rule used above: with member k taking cost[k] / b on b

@@ -21,4 +21,19 @@ int members_reset(const SimParams* dmembers, int n, unsigned* dfill, cudaStream_
 // launch's error flag, else 0) to dout[n] (enqueued on st)
 int members_status(const SimParams* dmembers, int n, int* dout, cudaStream_t st);
 
+// One member's slice of an ensemble state transfer: its six state fields
+// (kernel instance stride Rk x N, the first R instances moved), T, dt and step,
+// at word `off` of the staging buffer ([6][R][N] doubles, then T[R], dt[R],
+// step[R] as 8-byte words)
+struct XferMember {
+    double* state6;
+    double* T;
+    double* dt;
+    int64_t* step;
+    int64_t off, N;
+    int R, Rk;
+};
+// dir 0: staging buffer -> members; 1: members -> staging buffer (enqueued on st)
+int members_xfer(const XferMember* dm, int n, double* stage, int dir, cudaStream_t st);
+
 }  // namespace qdfn

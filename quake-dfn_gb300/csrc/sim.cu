@@ -945,9 +945,14 @@ struct qdfn_ensemble {
     int* hstat = nullptr;                // pinned [n]
     unsigned* dfill = nullptr;           // device: members that have taken their steps (fill mode)
     int fill = 0;                        // fill mode on
+    XferMember* dxfer = nullptr;         // device [n]: the members' slices of a state transfer
+    double* dstage = nullptr;            // device: staging buffer of qdfn_ensemble_{set,get}_state_all
+    int64_t stage_words = 0;
     cudaStream_t pending = nullptr;
     bool running = false;
     ~qdfn_ensemble() {
+        if (dxfer) cudaFree(dxfer);
+        if (dstage) cudaFree(dstage);
         if (hparams) cudaFreeHost(hparams);
         if (hstat) cudaFreeHost(hstat);
         if (dfill) cudaFree(dfill);
@@ -1111,6 +1116,21 @@ extern "C" int qdfn_ensemble_create(qdfn_ensemble** out, int n, qdfn_ctx* const*
                 cudaMalloc(&e->dfill, sizeof(unsigned)) != cudaSuccess))
         rc = fail(QDFN_ERR_NOMEM, "ensemble buffers");
     if (!rc) rc = ensemble_configure(e);
+    if (!rc) {   // the state-transfer map: member after member, [6][R][N] then T, dt, step [R]
+        std::vector<XferMember> xm(n);
+        int64_t off = 0;
+        for (int k = 0; k < n; ++k) {
+            qdfn_ctx* c = members[k];
+            xm[k] = XferMember{c->V, c->T, c->dt, c->step, off, c->N, c->R, kernel_R(c->R)};
+            off += 6 * (int64_t)c->R * c->N + 3 * (int64_t)c->R;
+        }
+        e->stage_words = off;
+        if (cudaMalloc(&e->dxfer, sizeof(XferMember) * n) != cudaSuccess ||
+            cudaMalloc(&e->dstage, sizeof(double) * (size_t)off) != cudaSuccess)
+            rc = fail(QDFN_ERR_NOMEM, "ensemble state buffers");
+        else if (cudaMemcpy(e->dxfer, xm.data(), sizeof(XferMember) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(QDFN_ERR_CUDA, "ensemble state map");
+    }
     if (rc) {
         for (qdfn_ctx* c : e->m) c->nblocks_override = 0;
         delete e;
@@ -1250,6 +1270,39 @@ extern "C" int qdfn_ensemble_sync(qdfn_ensemble* e) {
     QDFN_CUDA(cudaStreamSynchronize(e->pending));
     for (size_t k = 0; k < e->m.size(); ++k)
         if (e->hstat[k] != 0) return fail(e->hstat[k], "ensemble member " + std::to_string(k) + " stopped");
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_ensemble_state_bytes(const qdfn_ensemble* e, int64_t* bytes) {
+    if (!e || !bytes) return fail(QDFN_ERR_INVALID, "null argument");
+    *bytes = e->stage_words * 8;
+    return QDFN_OK;
+}
+
+extern "C" int qdfn_ensemble_set_state_all(qdfn_ensemble* e, const void* host, void* stream) {
+    int rc = ensemble_check(e);
+    if (rc) return rc;
+    if (!host) return fail(QDFN_ERR_INVALID, "null host buffer");
+    if (e->running) return fail(QDFN_ERR_STATE, "a run is in flight (qdfn_ensemble_get_state_all first)");
+    cudaStream_t st = (cudaStream_t)stream;
+    QDFN_CUDA(cudaMemcpyAsync(e->dstage, host, (size_t)e->stage_words * 8, cudaMemcpyHostToDevice, st));
+    return members_xfer(e->dxfer, (int)e->m.size(), e->dstage, 0, st);
+}
+
+extern "C" int qdfn_ensemble_get_state_all(qdfn_ensemble* e, void* host, void* stream, int wait) {
+    if (!e || !host) return fail(QDFN_ERR_INVALID, "null argument");
+    for (size_t k = 0; k < e->m.size(); ++k)
+        if (!e->m[k]) return fail(QDFN_ERR_STATE, "member " + std::to_string(k) + " was destroyed");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool completes = e->running && e->pending == st;
+    if (e->running && !completes) return fail(QDFN_ERR_STATE, "the run in flight is on another stream");
+    if (completes && !wait) return fail(QDFN_ERR_INVALID, "reading the state of a run in flight needs wait=1");
+    int rc = members_xfer(e->dxfer, (int)e->m.size(), e->dstage, 1, st);
+    if (rc) return rc;
+    QDFN_CUDA(cudaMemcpyAsync(host, e->dstage, (size_t)e->stage_words * 8, cudaMemcpyDeviceToHost, st));
+    if (!wait) return QDFN_OK;
+    if (completes) return qdfn_ensemble_sync(e);   // the run's outcome arrived with the state
+    QDFN_CUDA(cudaStreamSynchronize(st));
     return QDFN_OK;
 }
 

@@ -36,6 +36,7 @@ EXPORTS = [
     "qdfn_ensemble_balance", "qdfn_ensemble_run", "qdfn_ensemble_run_async", "qdfn_ensemble_sync",
     "qdfn_ensemble_shares", "qdfn_ensemble_set_fill", "qdfn_check_division", "qdfn_adjoint_run",
     "qdfn_assemble_tri_pairs_dev", "qdfn_set_early_cols", "qdfn_get_early_cols",
+    "qdfn_ensemble_state_bytes", "qdfn_ensemble_set_state_all", "qdfn_ensemble_get_state_all",
 ]
 
 
@@ -130,6 +131,9 @@ def load():
     L.qdfn_ensemble_sync.argtypes = [C.c_void_p]
     L.qdfn_ensemble_shares.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p]
     L.qdfn_ensemble_set_fill.argtypes = [C.c_void_p, C.c_int]
+    L.qdfn_ensemble_state_bytes.argtypes = [C.c_void_p, _ip]
+    L.qdfn_ensemble_set_state_all.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qdfn_ensemble_get_state_all.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
     L.qdfn_check_division.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.qdfn_assemble_tri_pairs_dev.argtypes = [C.c_int64] + [C.c_void_p] * 9 + [C.c_double, C.c_double] + \
                                              [C.c_void_p] * 3

@@ -18,6 +18,11 @@ import numpy as np
 from . import _lib, simulate
 
 
+def _ptr(buf):
+    """Address of a host buffer: a numpy array or a CPU tensor."""
+    return buf.data_ptr() if hasattr(buf, "data_ptr") else buf.ctypes.data
+
+
 def sm_shares(cost, n_sms):
     """Blocks per member: at least one each, minimising the longest member
     time cost/blocks, summing to ``n_sms`` -- the library's split rule
@@ -92,6 +97,60 @@ class Ensemble:
             self.balance()
             hist.append(self.blocks.copy())
         return hist
+
+    # -- the whole ensemble's state in one copy each way -------------------
+    def state_words(self):
+        """8-byte words of the ensemble's state record (qdfn_ensemble_state_bytes / 8)."""
+        n = C.c_int64()
+        _lib.check(self.L.qdfn_ensemble_state_bytes(self._h, C.byref(n)))
+        return int(n.value) // 8
+
+    def pack_states(self, states, out=None):
+        """The state record from per-member, per-instance state dicts (as
+        Simulation.state returns): member after member, [6][n_inst][N] (V, D,
+        theta, friction, accel, sigma_old), then T, dt, step [n_inst].  `out`:
+        a float64 buffer (numpy array or CPU tensor) of state_words() words."""
+        buf = np.empty(self.state_words()) if out is None else out
+        a = buf.numpy() if hasattr(buf, "numpy") else buf
+        o = 0
+        for sim, sts in zip(self.members, states):
+            R, N = sim.n_inst, sim.N
+            for k in simulate.Simulation.STATE_FIELDS:
+                a[o:o + R * N] = np.concatenate([st[k] for st in sts])
+                o += R * N
+            a[o:o + R] = [st["T"] for st in sts]
+            a[o + R:o + 2 * R] = [st["dt"] for st in sts]
+            a[o + 2 * R:o + 3 * R].view(np.int64)[:] = [st["step"] for st in sts]
+            o += 3 * R
+        return buf
+
+    def unpack_states(self, buf):
+        """Per-member lists of per-instance state dicts from a state record."""
+        a = buf.numpy() if hasattr(buf, "numpy") else np.asarray(buf)
+        out, o = [], 0
+        for sim in self.members:
+            R, N = sim.n_inst, sim.N
+            f = {}
+            for k in simulate.Simulation.STATE_FIELDS:
+                f[k] = a[o:o + R * N].reshape(R, N).copy()
+                o += R * N
+            T, dt, step = a[o:o + R], a[o + R:o + 2 * R], a[o + 2 * R:o + 3 * R].view(np.int64)
+            o += 3 * R
+            out.append([dict({k: f[k][r] for k in f}, T=float(T[r]), dt=float(dt[r]), step=int(step[r]))
+                        for r in range(R)])
+        return out
+
+    def set_state_all(self, buf, stream=None):
+        """Every member's state from one host buffer (state record; pinned for
+        an asynchronous copy), one copy (qdfn_ensemble_set_state_all)."""
+        _lib.check(self.L.qdfn_ensemble_set_state_all(self._h, C.c_void_p(_ptr(buf)),
+                                                      C.c_void_p(stream) if stream else None))
+
+    def get_state_all(self, buf, stream=None, wait=True):
+        """Every member's state into one host buffer, one copy; with wait it
+        also completes a run in flight on the same stream."""
+        _lib.check(self.L.qdfn_ensemble_get_state_all(self._h, C.c_void_p(_ptr(buf)),
+                                                      C.c_void_p(stream) if stream else None, 1 if wait else 0))
 
     def set_fill(self, on=True):
         """Fill mode: members that have taken the run's nsteps keep stepping

@@ -168,3 +168,51 @@ def test_ensemble_rejects_mixed_members_and_member_runs_in_flight(qdfn_mod):
     ens.set_blocks([2, 3])
     assert 1 <= ens.blocks[0] <= 2 and 1 <= ens.blocks[1] <= 3   # (small members use fewer)
     ens.close()
+
+
+@pytest.mark.gpu
+def test_one_copy_state_transfer_matches_the_members(qdfn_mod):
+    """qdfn_ensemble_{set,get}_state_all: the whole ensemble's state in one
+    host buffer.  Setting a packed record puts every member's state in place
+    (what each member's own calls read back, bit for bit); after a run, the
+    record read back is every member's state; a run in flight on the stream is
+    completed by the read; setting during a run is refused."""
+    import torch
+    from qdfn import _lib, ensemble
+    built = [_member(seed, R, n_faults=3) for seed, R in ((5, 4), (6, 3), (7, 4))]
+    ens = ensemble.Ensemble([m for m, _ in built], precision="fp32")
+    ens.run(20, timeout_s=60)
+    snap = [[sim.state(r) for r in range(sim.n_inst)] for sim in ens.members]
+    ens.run(15, timeout_s=60)
+    buf = torch.empty(ens.state_words(), dtype=torch.float64).pin_memory()
+    assert ens.state_words() == sum(6 * sim.n_inst * sim.N + 3 * sim.n_inst for sim in ens.members)
+    ens.pack_states(snap, out=buf)
+    ens.set_state_all(buf)
+    torch.cuda.synchronize()
+    for sim, sts in zip(ens.members, snap):
+        for r, st in enumerate(sts):
+            got = sim.state(r)
+            assert got["step"] == st["step"] == 20 and got["T"] == st["T"] and got["dt"] == st["dt"]
+            for k in ensemble.simulate.Simulation.STATE_FIELDS:
+                assert np.array_equal(got[k], st[k]), k
+    st = torch.cuda.Stream()
+    ens.run_async(15, timeout_s=60, stream=st.cuda_stream)
+    with pytest.raises(_lib.QdfnError):
+        ens.set_state_all(buf, stream=st.cuda_stream)
+    ens.get_state_all(buf, stream=st.cuda_stream, wait=True)   # completes the run
+    back = ens.unpack_states(buf)
+    for sim, sts in zip(ens.members, back):
+        for r, rec in enumerate(sts):
+            own = sim.state(r)
+            assert rec["step"] == own["step"] == 35 and rec["T"] == own["T"] and rec["dt"] == own["dt"]
+            for k in ensemble.simulate.Simulation.STATE_FIELDS:
+                assert np.array_equal(rec[k], own[k]), k
+    # the same 15 steps from the restored state give the same record
+    ens.pack_states(snap, out=buf)
+    ens.set_state_all(buf)
+    ens.run(15, timeout_s=60)
+    again = [[sim.state(r) for r in range(sim.n_inst)] for sim in ens.members]
+    for a, b in zip(again, back):
+        for x, y in zip(a, b):
+            assert x["T"] == y["T"] and np.array_equal(x["D"], y["D"])
+    ens.close()
