@@ -22,8 +22,10 @@ __global__ void k_members_reset(const SimParams* __restrict__ members, int n, un
 }
 
 // one thread per member: the first failing instance's status, else the
-// launch's error flag, else 0
-__global__ void k_members_status(const SimParams* __restrict__ members, int n, int* __restrict__ out) {
+// launch's error flag, else 0; and the member's busy ns so far (the
+// autotuner's measure, read back with the status instead of member by member)
+__global__ void k_members_status(const SimParams* __restrict__ members, int n, int* __restrict__ out,
+                                 unsigned long long* __restrict__ busy) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
     const SimParams& p = members[m];
@@ -31,6 +33,7 @@ __global__ void k_members_status(const SimParams* __restrict__ members, int n, i
     for (int r = 0; r < p.R && s == 0; ++r) s = p.status[r];
     if (s == 0) s = p.gerr[0];
     out[m] = s;
+    busy[m] = p.prof ? p.prof[0] + p.prof[1] + p.prof[2] + p.prof[3] : 0ull;
 }
 
 // the state of every member to or from one staging buffer: blockIdx.y is the
@@ -83,8 +86,8 @@ int members_xfer(const XferMember* dm, int n, double* stage, int dir, cudaStream
     return QDFN_OK;
 }
 
-int members_status(const SimParams* dmembers, int n, int* dout, cudaStream_t st) {
-    k_members_status<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n, dout);
+int members_status(const SimParams* dmembers, int n, int* dout, unsigned long long* dbusy, cudaStream_t st) {
+    k_members_status<<<(n + 127) / 128, 128, 0, st>>>(dmembers, n, dout, dbusy);
     QDFN_CUDA(cudaGetLastError());
     return QDFN_OK;
 }

@@ -18,8 +18,9 @@ MembersKernel members_kernel(int prec, int R);
 // counter when dfill is not null (enqueued on st)
 int members_reset(const SimParams* dmembers, int n, unsigned* dfill, cudaStream_t st);
 // writes every member's outcome (first failing instance status, else the
-// launch's error flag, else 0) to dout[n] (enqueued on st)
-int members_status(const SimParams* dmembers, int n, int* dout, cudaStream_t st);
+// launch's error flag, else 0) to dout[n] and its cumulative busy ns (block
+// 0's phase counters) to dbusy[n] (enqueued on st)
+int members_status(const SimParams* dmembers, int n, int* dout, unsigned long long* dbusy, cudaStream_t st);
 
 // One member's slice of an ensemble state transfer: its six state fields
 // (kernel instance stride Rk x N, the first R instances moved), T, dt and step,

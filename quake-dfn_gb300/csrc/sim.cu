@@ -558,11 +558,13 @@ extern "C" int qdfn_set_external_stress(qdfn_ctx* c, int64_t nt, const double* t
 
 namespace {
 bool ensemble_running(const qdfn_ensemble* e);
+void ensemble_member_ran(qdfn_ensemble* e);
 }
 
 extern "C" int qdfn_run_async(qdfn_ctx* c, int64_t nsteps, double timeout_s, void* stream) {
     if (!c) return fail(QDFN_ERR_INVALID, "null context");
     if (c->ens && ensemble_running(c->ens)) return fail(QDFN_ERR_STATE, "the context's ensemble has a run in flight");
+    if (c->ens) ensemble_member_ran(c->ens);   // its busy time moves outside the ensemble's readback
     if (c->prec < 0) return fail(QDFN_ERR_STATE, "no operator set (qdfn_set_dense first)");
     if (nsteps < 0) return fail(QDFN_ERR_INVALID, "nsteps < 0");
     if (nsteps == 0) return QDFN_OK;
@@ -940,9 +942,14 @@ struct qdfn_ensemble {
     size_t smem = 0;
     SimParams* hparams = nullptr;        // pinned [n]
     SimParams* dparams = nullptr;        // device [n]
-    int2* dmap = nullptr;                // device [total]: (member, block within it)
+    int2* dmap = nullptr;                // device [map_cap]: (member, block within it)
+    size_t map_cap = 0;
+    std::vector<int> configured;         // share each member was last configured for (0: never)
     int* dstat = nullptr;                // device [n] outcome of the last run
     int* hstat = nullptr;                // pinned [n]
+    unsigned long long* dbusy = nullptr; // device [n] members' busy ns after the last run
+    unsigned long long* hbusy = nullptr; // pinned [n]
+    bool busy_valid = false;             // hbusy is current (the last run's, read back)
     unsigned* dfill = nullptr;           // device: members that have taken their steps (fill mode)
     int fill = 0;                        // fill mode on
     XferMember* dxfer = nullptr;         // device [n]: the members' slices of a state transfer
@@ -955,6 +962,8 @@ struct qdfn_ensemble {
         if (dstage) cudaFree(dstage);
         if (hparams) cudaFreeHost(hparams);
         if (hstat) cudaFreeHost(hstat);
+        if (hbusy) cudaFreeHost(hbusy);
+        if (dbusy) cudaFree(dbusy);
         if (dfill) cudaFree(dfill);
         if (dparams) cudaFree(dparams);
         if (dmap) cudaFree(dmap);
@@ -965,6 +974,7 @@ struct qdfn_ensemble {
 namespace {
 
 bool ensemble_running(const qdfn_ensemble* e) { return e->running; }
+void ensemble_member_ran(qdfn_ensemble* e) { e->busy_valid = false; }
 
 void ensemble_detach(qdfn_ensemble* e, qdfn_ctx* c) {
     for (auto& x : e->m)
@@ -980,6 +990,9 @@ double member_cost(const qdfn_ctx* c) {
     const double n = (double)c->N;
     return 2.0 * n * n * esz / 44.0 + 450.0 * kernel_R(c->R) * n;
 }
+
+// A member's busy ns as the status kernel of the last ensemble run read them.
+uint64_t busy_of(const qdfn_ensemble* e, int k) { return (uint64_t)e->hbusy[k]; }
 
 // Member busy time of its runs so far (block 0's phase counters), ns.
 uint64_t member_busy_ns(const qdfn_ctx* c) {
@@ -1003,11 +1016,15 @@ int ensemble_configure(qdfn_ensemble* e) {
     const int n = (int)e->m.size();
     size_t smem = 0;
     int total = 0;
+    e->configured.resize(n, 0);
     for (int k = 0; k < n; ++k) {
         qdfn_ctx* c = e->m[k];
-        c->nblocks_override = e->share[k];
-        int rc = configure_launch(c);
-        if (rc) return rc;
+        if (e->configured[k] != e->share[k] || c->nblocks_override != e->share[k]) {
+            c->nblocks_override = e->share[k];
+            int rc = configure_launch(c);
+            if (rc) return rc;
+            e->configured[k] = e->share[k];
+        }
         smem = std::max(smem, c->smem);
         total += c->nblocks;
     }
@@ -1021,9 +1038,12 @@ int ensemble_configure(qdfn_ensemble* e) {
     map.reserve(total);
     for (int k = 0; k < n; ++k)
         for (int b = 0; b < e->m[k]->nblocks; ++b) map.push_back(make_int2(k, b));
-    if (e->dmap) cudaFree(e->dmap);
-    e->dmap = nullptr;
-    QDFN_CUDA(cudaMalloc(&e->dmap, sizeof(int2) * map.size()));
+    if (map.size() > e->map_cap) {   // kept across re-divisions: sized for the largest grid
+        if (e->dmap) cudaFree(e->dmap);
+        e->dmap = nullptr;
+        e->map_cap = std::max(map.size(), (size_t)cap);
+        QDFN_CUDA(cudaMalloc(&e->dmap, sizeof(int2) * e->map_cap));
+    }
     QDFN_CUDA(cudaMemcpy(e->dmap, map.data(), sizeof(int2) * map.size(), cudaMemcpyHostToDevice));
     e->total = total;
     e->smem = smem;
@@ -1111,6 +1131,8 @@ extern "C" int qdfn_ensemble_create(qdfn_ensemble** out, int n, qdfn_ctx* const*
     }
     if (!rc && (cudaMallocHost(&e->hparams, sizeof(SimParams) * n) != cudaSuccess ||
                 cudaMallocHost(&e->hstat, sizeof(int) * n) != cudaSuccess ||
+                cudaMallocHost(&e->hbusy, sizeof(unsigned long long) * n) != cudaSuccess ||
+                cudaMalloc(&e->dbusy, sizeof(unsigned long long) * n) != cudaSuccess ||
                 cudaMalloc(&e->dparams, sizeof(SimParams) * n) != cudaSuccess ||
                 cudaMalloc(&e->dstat, sizeof(int) * n) != cudaSuccess ||
                 cudaMalloc(&e->dfill, sizeof(unsigned)) != cudaSuccess))
@@ -1199,7 +1221,7 @@ extern "C" int qdfn_ensemble_balance(qdfn_ensemble* e) {
     std::vector<uint64_t> now(n);
     bool any = false;
     for (int k = 0; k < n; ++k) {
-        now[k] = member_busy_ns(e->m[k]);
+        now[k] = e->busy_valid ? busy_of(e, k) : member_busy_ns(e->m[k]);
         const double t = (double)(now[k] - e->mark[k]);
         cost[k] = t * e->m[k]->nblocks;
         any = any || t > 0;
@@ -1256,8 +1278,10 @@ extern "C" int qdfn_ensemble_run_async(qdfn_ensemble* e, int64_t nsteps, double 
     const int2* dm = e->dmap;
     void* args[] = {&dp, &dm, &nsteps};
     QDFN_CUDA(cudaLaunchCooperativeKernel((const void*)k, dim3(e->total), dim3(kSimThreads), args, e->smem, st));
-    if ((rc = members_status(e->dparams, n, e->dstat, st))) return rc;
+    if ((rc = members_status(e->dparams, n, e->dstat, e->dbusy, st))) return rc;
     QDFN_CUDA(cudaMemcpyAsync(e->hstat, e->dstat, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    QDFN_CUDA(cudaMemcpyAsync(e->hbusy, e->dbusy, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, st));
+    e->busy_valid = false;   // current once the run is synchronised
     e->pending = st;
     e->running = true;
     return QDFN_OK;
@@ -1268,6 +1292,7 @@ extern "C" int qdfn_ensemble_sync(qdfn_ensemble* e) {
     if (!e->running) return QDFN_OK;
     e->running = false;
     QDFN_CUDA(cudaStreamSynchronize(e->pending));
+    e->busy_valid = true;
     for (size_t k = 0; k < e->m.size(); ++k)
         if (e->hstat[k] != 0) return fail(e->hstat[k], "ensemble member " + std::to_string(k) + " stopped");
     return QDFN_OK;
