@@ -10,7 +10,9 @@
 // The product runs in two passes inside the persistent kernel, as WARP tasks
 // handed out in a fixed order over every warp of the grid (tree leaves hold at
 // most `leaf` patches, so near-field blocks are small and a block per CTA
-// would leave most threads idle):
+// would leave most threads idle); pass B starts with the dense blocks, which
+// need nothing from pass A, and waits on a completion count of pass A (not on
+// a grid barrier) before its low-rank blocks:
 //   A: t_b[kk] = Vt_b[kk,:] x[src]    one task per (low-rank block, group of
 //                                     rank rows): lanes stride the rows,
 //                                     coalesced, warp sums
@@ -44,8 +46,10 @@ struct Ops {
     const void* store;       // element storage
     const int64_t* lr_list;  // pass-A tasks: (blk index << 8) | first rank row of the group
     int64_t n_lr;
-    const int64_t* tile_list;   // pass-B tasks: (blk index << 20) | 64-row slice
+    const int64_t* tile_list;   // pass-B tasks: (blk index << 20) | 64-row slice; dense blocks' first
     int64_t n_tiles;
+    int64_t n_tiles_dense;      // the first n_tiles_dense tasks are dense blocks' (need no pass A)
+    unsigned long long* a_done; // pass-A tasks completed since the launch began (monotone)
     double* t;               // low-rank intermediates
     double* part;            // [slots][R]
     const int64_t* rowptr;   // [2][N+1] CSR over receiver rows (shear, normal)
@@ -154,6 +158,7 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
     const int64_t W = warps_global(), w = warp_id_global();
     int64_t k = 0, q = snake_task(0, w, W);
     int64_t code = q < h.n_lr ? __ldg(h.lr_list + q) : 0;
+    unsigned long long done = 0;
     while (q < h.n_lr) {
         const Blk b = load_blk(h.blk + (code >> 8));
         const int kk0 = (int)(code & 255);
@@ -206,26 +211,38 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
         }
         q = qn;
         code = code_n;
+        ++done;
     }
+    // publish this warp's tasks: every lane fences its own t stores first
+    __threadfence();
+    __syncwarp();
+    if (lane == 0 && done > 0 && h.a_done) atomicAdd(h.a_done, done);
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_ull(const unsigned long long* ptr) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ptr) : "memory");
+    return v;
 }
 
 // pass B: per receiver-row partials of every block, 64-row slices per warp
 // (a lane per two rows).  The inner values (x of the block's sources, or t)
 // are held by the lanes and broadcast by shuffles; the matrix columns are
-// loaded eight at a time before they are used
+// loaded eight at a time before they are used.  Tasks [lo, hi) of the list.
 template <class T, int R>
-__device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*) {
+__device__ void pass_b_range(const Ops& h, const double* __restrict__ D, int64_t N, int64_t lo, int64_t hi) {
     constexpr int U = 8;
     const int lane = threadIdx.x & 31;
     const T* st = reinterpret_cast<const T*>(h.store);
     const int64_t W = warps_global(), w = warp_id_global();
+    const int64_t n = hi - lo;
     int64_t k = 0, q = snake_task(0, w, W);
-    int64_t code = q < h.n_tiles ? __ldg(h.tile_list + q) : 0;
-    while (q < h.n_tiles) {
+    int64_t code = q < n ? __ldg(h.tile_list + lo + q) : 0;
+    while (q < n) {
         const Blk b = load_blk(h.blk + (code >> 20));
         const int64_t i0 = (code & ((1 << 20) - 1)) * kSliceRows;
         const int64_t qn = snake_task(++k, w, W);
-        const int64_t code_n = qn < h.n_tiles ? __ldg(h.tile_list + qn) : 0;
+        const int64_t code_n = qn < n ? __ldg(h.tile_list + lo + qn) : 0;
         const int64_t ia = i0 + lane, ib = i0 + 32 + lane;
         const bool va = ia < b.nr, vb = ib < b.nr;
         T sa[R], sb[R];
@@ -273,6 +290,34 @@ __device__ void pass_b(const Ops& h, const double* __restrict__ D, int64_t N, T*
         q = qn;
         code = code_n;
     }
+}
+
+// Pass B of a step: the dense blocks' tasks first (they need no pass-A
+// result, so they fill the time while the last pass-A tasks finish), then a
+// bounded wait until a_done reaches a_target (every pass-A task of this step
+// has published its t), then the low-rank blocks' tasks.  a_target = 0: no
+// wait (pass A ran in an earlier launch).  Returns false if the wait gave up
+// (limit_ns, or another block's error in *gerr).
+template <class T, int R>
+__device__ bool pass_b(const Ops& h, const double* __restrict__ D, int64_t N, unsigned long long a_target,
+                       uint64_t limit_ns, const int* gerr) {
+    pass_b_range<T, R>(h, D, N, 0, h.n_tiles_dense);
+    if (h.n_tiles <= h.n_tiles_dense) return true;
+    int ok = 1;
+    if (a_target > 0 && (threadIdx.x & 31) == 0 && ld_acquire_ull(h.a_done) < a_target) {
+        uint64_t t0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        while (ld_acquire_ull(h.a_done) < a_target) {
+            uint64_t t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t - t0 > limit_ns || *(volatile const int*)gerr != 0) { ok = 0; break; }
+            __nanosleep(128);
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) return false;
+    pass_b_range<T, R>(h, D, N, h.n_tiles_dense, h.n_tiles);
+    return true;
 }
 
 // sum of the partials of receiver row i (side 0 shear, 1 normal), block order;

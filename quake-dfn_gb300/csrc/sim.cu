@@ -1690,7 +1690,14 @@ extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, c
         return x.first != y.first ? x.first > y.first : x.second < y.second;
     };
     std::sort(ta.begin(), ta.end(), by_cost);
-    std::sort(tb.begin(), tb.end(), by_cost);
+    // pass B: the dense blocks' tasks first (they need nothing from pass A),
+    // each part largest first
+    std::stable_partition(tb.begin(), tb.end(),
+                          [&](const std::pair<int64_t, int64_t>& x) { return blk[x.second >> 20].rank < 0; });
+    const int64_t n_dense = (int64_t)std::count_if(
+        tb.begin(), tb.end(), [&](const std::pair<int64_t, int64_t>& x) { return blk[x.second >> 20].rank < 0; });
+    std::sort(tb.begin(), tb.begin() + n_dense, by_cost);
+    std::sort(tb.begin() + n_dense, tb.end(), by_cost);
     std::vector<int64_t> lr, tiles;
     for (auto& x : ta) lr.push_back(x.second);
     for (auto& x : tb) tiles.push_back(x.second);
@@ -1712,6 +1719,8 @@ extern "C" int qdfn_set_hmatrix(qdfn_ctx* c, int64_t nb, const int64_t* range, c
     hmat::Ops& h = c->hops;
     h.blk = dblk; h.nb = nb; h.store = dstore; h.lr_list = dlr; h.n_lr = (int64_t)lr.size();
     h.tile_list = dtiles; h.n_tiles = (int64_t)tiles.size(); h.t = dt; h.part = dpart;
+    h.n_tiles_dense = n_dense;
+    h.a_done = c->tile_ctr;   // reset in every launch's prologue
     h.rowptr = drp; h.rowslot = drs;
     c->prec = precision;
     c->hmat = 1;

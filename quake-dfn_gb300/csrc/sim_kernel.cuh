@@ -1349,8 +1349,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
         if constexpr (HM) {
             const double* Dcur = par ? p.Dn : p.D;
             hmat::pass_a<X, R>(p.h, Dcur, N, xs, hacc);
-            if (!grid_barrier(p, deadline)) return;
-            hmat::pass_b<X, R>(p.h, Dcur, N, xs);
+            // pass B's low-rank tasks wait for this step's pass-A count, not a grid barrier
+            if (!hmat::pass_b<X, R>(p.h, Dcur, N, (unsigned long long)(it + 1) * (unsigned long long)p.h.n_lr,
+                                    kWaitLimitNs, p.gerr))
+                atomicExch(p.gerr, QDFN_ERR_TIMEOUT);
             if (!grid_barrier(p, deadline)) return;
         } else if constexpr (sizeof(X) == 8) {
             // FP64 storage: the operator's FMAs already load the FP64 pipe that
@@ -1842,7 +1844,7 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_hmat_a(SimParams p) {
 template <class X, int R>
 __global__ void __launch_bounds__(kSimThreads, 1) k_hmat_b(SimParams p) {
     extern __shared__ unsigned char smem_raw[];
-    hmat::pass_b<X, R>(p.h, p.D, p.N, reinterpret_cast<X*>(smem_raw));
+    hmat::pass_b<X, R>(p.h, p.D, p.N, 0ull, kWaitLimitNs, p.gerr);   // pass A ran in the launch before
 }
 template <int R>
 __global__ void k_hmat_rows(SimParams p) {
