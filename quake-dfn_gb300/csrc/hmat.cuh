@@ -343,5 +343,49 @@ __device__ __forceinline__ double row_sum(const Ops& h, int side, int64_t N, int
     return s;
 }
 
+// The products of a block's solve items q0..q1-1 (q = r N + i) for a step's
+// first solve pass, by the whole block before its solves: four threads per
+// (item, matrix), each summing every fourth partial of the row in block
+// order, combined as (p0 + p1) + (p2 + p3) -- a fixed order, so results are
+// reproducible; the solves then read tld and knd.  Every thread of the block
+// runs the same rounds (the shuffles need whole warps).
+template <int R>
+__device__ void row_sums_block(const Ops& h, int64_t N, const double* __restrict__ kself, double* __restrict__ tld,
+                               double* __restrict__ knd, int64_t q0, int64_t q1) {
+    const int64_t work = (q1 - q0) * 8;
+    for (int64_t base = 0; base < work; base += blockDim.x) {
+        const int64_t t = base + threadIdx.x;
+        const bool valid = t < work;
+        const int sub = (int)(t & 3), side = (int)((t >> 2) & 1);
+        double acc = 0.0;
+        int64_t q = 0, i = 0;
+        if (valid) {
+            q = q0 + (t >> 3);
+            const int r = (int)(q / N);
+            i = q - (int64_t)r * N;
+            const int64_t* rp = h.rowptr + side * (N + 1);
+            const int64_t e = __ldg(rp + i + 1);
+            int64_t k = __ldg(rp + i) + sub;
+            for (; k + 12 < e; k += 16) {   // four of this thread's partials at a time, loaded before added
+                int64_t sl[4];
+                double v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) sl[u] = __ldg(h.rowslot + k + 4 * u);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = __ldcg(h.part + sl[u] * R + r);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc += v[u];
+            }
+            for (; k < e; k += 4) acc += __ldcg(h.part + __ldg(h.rowslot + k) * R + r);
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (valid && sub == 0) {
+            if (side == 0) tld[q] = (-acc) / -kself[i];   // main_H :241-248: H_load (0 - D) ./ -K_Self
+            else knd[q] = acc;                           // H_n D
+        }
+    }
+}
+
 }  // namespace hmat
 }  // namespace qdfn

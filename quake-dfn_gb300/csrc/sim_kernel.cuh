@@ -1616,10 +1616,18 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
                 // sets the pass time
                 const int64_t per_cta = ((int64_t)R * N + p.nblk - 1) / p.nblk;
                 const int64_t q_end = min((int64_t)R * N, (int64_t)blk * per_cta + per_cta);
+                bool prod_here = first != 0;   // the solve item forms its own row's products
+                if constexpr (HM) {
+                    if (first) {   // the block's row sums first, spread over all its threads
+                        hmat::row_sums_block<R>(p.h, N, p.kself, p.tld, p.knd, (int64_t)blk * per_cta, q_end);
+                        __syncthreads();
+                        prod_here = false;
+                    }
+                }
                 for (int64_t q = (int64_t)blk * per_cta + threadIdx.x; q < q_end; q += kSimThreads) {
                     const int r = (int)(q / N);
                     if (s_done[r]) continue;
-                    solve_item(q, r, q - (int64_t)r * N, first != 0, false);
+                    solve_item(q, r, q - (int64_t)r * N, prod_here, false);
                 }
             }
             if (!HM && blk == 0 && (first || s_iter == 1)) {
