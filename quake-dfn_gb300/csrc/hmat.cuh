@@ -147,12 +147,15 @@ __device__ __forceinline__ void warp_sums(T (&hi)[G][R], T (&lo)[G][R], int lane
 
 // pass A: t_b = Vt_b x[src], one task per (low-rank block, group of up to
 // rows_a rank rows): the lanes stride the block's source range, each load of
-// x serving every row of the group, and each round issues the group's rows x 2
+// x serving every row of the group, and each round issues the group's rows x 4
 // column loads before any of them is used (HBM latency is hidden by the loads
 // in flight, not by occupancy: one 16-warp CTA per SM)
 template <class T, int R>
 __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*, double*) {
     constexpr int G = rows_a<R>();
+    // 32-column rounds per batch (G x kUA loads per lane in flight), within the
+    // persistent kernel's 128 registers
+    constexpr int kUA = (sizeof(T) == 4 && R == 1) ? 4 : 2;
     const int lane = threadIdx.x & 31;
     const T* st = reinterpret_cast<const T*>(h.store);
     const int64_t W = warps_global(), w = warp_id_global();
@@ -174,10 +177,10 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
         for (int g = 0; g < G; ++g)
 #pragma unroll
             for (int r = 0; r < R; ++r) { hi[g][r] = 0; lo[g][r] = 0; }
-        for (int64_t j0 = 0; j0 < b.ns; j0 += 64) {
-            T v[2][G], xv[2][R];
+        for (int64_t j0 = 0; j0 < b.ns; j0 += 32 * kUA) {
+            T v[kUA][G], xv[kUA][R];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
+            for (int u = 0; u < kUA; ++u) {
                 const int64_t j = j0 + u * 32 + lane;
                 const bool ok = j < b.ns;
 #pragma unroll
@@ -186,7 +189,7 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
                 for (int r = 0; r < R; ++r) xv[u][r] = ok ? (T)__ldcg(xs + (int64_t)r * N + j) : (T)0;
             }
 #pragma unroll
-            for (int u = 0; u < 2; ++u)
+            for (int u = 0; u < kUA; ++u)
 #pragma unroll
                 for (int g = 0; g < G; ++g)
 #pragma unroll
@@ -228,10 +231,10 @@ __device__ __forceinline__ unsigned long long ld_acquire_ull(const unsigned long
 // pass B: per receiver-row partials of every block, 64-row slices per warp
 // (a lane per two rows).  The inner values (x of the block's sources, or t)
 // are held by the lanes and broadcast by shuffles; the matrix columns are
-// loaded eight at a time before they are used.  Tasks [lo, hi) of the list.
+// loaded sixteen at a time before they are used.  Tasks [lo, hi) of the list.
 template <class T, int R>
 __device__ void pass_b_range(const Ops& h, const double* __restrict__ D, int64_t N, int64_t lo, int64_t hi) {
-    constexpr int U = 8;
+    constexpr int U = sizeof(T) == 4 ? 16 : 8;   // columns loaded per batch: 2 x U loads per lane in flight
     const int lane = threadIdx.x & 31;
     const T* st = reinterpret_cast<const T*>(h.store);
     const int64_t W = warps_global(), w = warp_id_global();
