@@ -145,6 +145,19 @@ __device__ __forceinline__ void warp_sums(T (&hi)[G][R], T (&lo)[G][R], int lane
     for (int r = 0; r < R; ++r) out[r] = sizeof(T) == 4 ? (double)hi[0][r] + (double)lo[0][r] : (double)hi[0][r];
 }
 
+// The fields of a block descriptor that pass A reads (five words).
+struct BlkA {
+    int64_t s0, ns, off_a, toff;
+    int rank;
+};
+__device__ __forceinline__ BlkA load_blk_a(const Blk* p) {
+    const long long* w = reinterpret_cast<const long long*>(p);
+    BlkA b;
+    b.s0 = __ldg(w); b.ns = __ldg(w + 1); b.off_a = __ldg(w + 4); b.toff = __ldg(w + 6);
+    b.rank = __ldg(reinterpret_cast<const int*>(w + 8));
+    return b;
+}
+
 // pass A: t_b = Vt_b x[src], one task per (low-rank block, group of up to
 // rows_a rank rows): the lanes stride the block's source range, each load of
 // x serving every row of the group, and each round issues the group's rows x 4
@@ -159,14 +172,20 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
     const int lane = threadIdx.x & 31;
     const T* st = reinterpret_cast<const T*>(h.store);
     const int64_t W = warps_global(), w = warp_id_global();
+    // the block descriptor of the next task is loaded while this one runs, and
+    // the task code of the one after it: a small task then costs one round trip
+    // (its data), not three (code, descriptor, data)
     int64_t k = 0, q = snake_task(0, w, W);
+    const int64_t q1 = snake_task(1, w, W);
     int64_t code = q < h.n_lr ? __ldg(h.lr_list + q) : 0;
+    int64_t code_n = q1 < h.n_lr ? __ldg(h.lr_list + q1) : 0;
+    BlkA b = load_blk_a(h.blk + (code >> 8));
     unsigned long long done = 0;
     while (q < h.n_lr) {
-        const Blk b = load_blk(h.blk + (code >> 8));
+        const int64_t qn = snake_task(++k, w, W), qnn = snake_task(k + 1, w, W);
+        const int64_t code_nn = qnn < h.n_lr ? __ldg(h.lr_list + qnn) : 0;
+        const BlkA bn = load_blk_a(h.blk + (code_n >> 8));
         const int kk0 = (int)(code & 255);
-        const int64_t qn = snake_task(++k, w, W);
-        const int64_t code_n = qn < h.n_lr ? __ldg(h.lr_list + qn) : 0;   // the next task's code, early
         const int nrow = min(G, b.rank - kk0);
         const T* row0 = st + b.off_a + (int64_t)kk0 * b.ns;
         const double* xs = D + b.s0;
@@ -214,6 +233,8 @@ __device__ void pass_a(const Ops& h, const double* __restrict__ D, int64_t N, T*
         }
         q = qn;
         code = code_n;
+        code_n = code_nn;
+        b = bn;
         ++done;
     }
     // publish this warp's tasks: every lane fences its own t stores first
