@@ -1373,9 +1373,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             if (!grid_barrier(p, deadline)) return;
         } else {
             // Operator and solve pass 0, overlapped.  Warps [0, kOpWarps) stream
-            // the operator tiles (HBM-bound); the solver warps take 16-row chunks
-            // of every row block whose column chunks are all in and solve them
-            // (FP64-bound), so the two share each SM.  In a step that streams
+            // the operator tiles (HBM-bound); the solver warps take row chunks
+            // (32 rows, one lane per patch; 16 on lane pairs) of every row block
+            // whose column chunks are all in and solve them (FP64-bound), so the
+            // two share each SM.  In a step that streams
             // ahead the operator warps then stream the next step's tiles; in the
             // last step of a launch they join the solving instead.  A row's
             // solve needs only its own operator products, so the result is the
