@@ -158,6 +158,27 @@ int qdfn_set_dense(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_t ld
 int qdfn_set_dense_dev(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_t ld, int layout,
                        int precision, void* stream);
 
+/* ---- H-matrix structure on the device ------------------------------------ */
+/* The cluster tree and block partition of an H-matrix operator, built on the
+ * GPU (replaces GroupAndSort_AllLevel / BuildHierarchy,
+ * scripts/Functions_Hmatrix.jl:1-212, whose k-means tree is randomly
+ * initialised).  centres: host [N][3] element centres.  The elements are
+ * ordered by the Morton key of their centre (21 bits per axis in the centres'
+ * bounding box; ties by index), every node of more than `leaf` elements splits
+ * its range in halves, and a (receiver node, source node) pair is a low-rank
+ * block when its boxes are apart (dist > 0) and max(diameter) <= eta * dist, a
+ * dense block when both nodes are leaves, and is split otherwise.
+ * qdfn_hstruct_get: perm [N] (element at each position), ranges [n_blocks][4]
+ * (source first, source last, receiver first, receiver last, inclusive,
+ * positions of the order -- the ElementRange_SR form, 0-based) and
+ * admissible [n_blocks] (1 low-rank), blocks ordered by receiver then source
+ * start.  Any pointer may be NULL. */
+typedef struct qdfn_hstruct qdfn_hstruct;
+int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* centres, int leaf, double eta);
+int qdfn_hstruct_sizes(const qdfn_hstruct* h, int64_t* n_blocks, int64_t* n_nodes);
+int qdfn_hstruct_get(const qdfn_hstruct* h, int64_t* perm, int64_t* ranges, int32_t* admissible);
+int qdfn_hstruct_destroy(qdfn_hstruct* h);
+
 /* H-matrix operator (Functions_Hmatrix.jl).  nb blocks; range is nb x 4
  * {src_begin, src_end, recv_begin, recv_end}, 0-based inclusive (the
  * reference's ElementRange_SR minus one).  For block b and each of the shear (s)

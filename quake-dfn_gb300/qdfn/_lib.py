@@ -37,6 +37,7 @@ EXPORTS = [
     "qdfn_ensemble_shares", "qdfn_ensemble_set_fill", "qdfn_check_division", "qdfn_adjoint_run",
     "qdfn_assemble_tri_pairs_dev", "qdfn_set_early_cols", "qdfn_get_early_cols",
     "qdfn_ensemble_state_bytes", "qdfn_ensemble_set_state_all", "qdfn_ensemble_get_state_all",
+    "qdfn_hstruct_build", "qdfn_hstruct_sizes", "qdfn_hstruct_get", "qdfn_hstruct_destroy",
 ]
 
 
@@ -98,6 +99,10 @@ def load():
     L.qdfn_set_dense.argtypes = [C.c_void_p, _dp, _dp, C.c_int64, C.c_int, C.c_int]
     L.qdfn_set_dense_dev.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p]
     L.qdfn_set_hmatrix.argtypes = [C.c_void_p, C.c_int64, _ip, _ip, _pdp, _pdp, _pdp, _ip, _pdp, _pdp, _pdp, C.c_int]
+    L.qdfn_hstruct_build.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_double]
+    L.qdfn_hstruct_sizes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qdfn_hstruct_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.qdfn_hstruct_destroy.argtypes = [C.c_void_p]
     L.qdfn_set_external_stress.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp]
     L.qdfn_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]
     L.qdfn_run_async.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]

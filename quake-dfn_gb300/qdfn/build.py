@@ -32,6 +32,7 @@ UNITS = {
     "noalloc.cu": ["--fmad=false"],
     "selfcheck.cu": ["--fmad=false"],
     "adjoint.cu": ["--fmad=false"],
+    "hstruct.cu": ["--fmad=false"],
 }
 
 

@@ -77,7 +77,8 @@ def block_partition(tree, eta=2.0):
     out = []
 
     def rec(t, s):
-        if max(tree.diam(t), tree.diam(s)) <= eta * tree.dist(t, s):
+        d = tree.dist(t, s)
+        if d > 0 and max(tree.diam(t), tree.diam(s)) <= eta * d:   # touching boxes: never admissible
             out.append((s, t, True))
             return
         ct, cs = tree.children[t], tree.children[s]
@@ -90,6 +91,48 @@ def block_partition(tree, eta=2.0):
 
     rec(0, 0)
     return out
+
+
+def device_partition(centres, leaf=64, eta=2.0):
+    """The cluster tree and block partition built on the GPU
+    (qdfn_hstruct_build: Morton order of the centres, halving tree,
+    admissibility dist > 0 and max(diam) <= eta * dist).  Returns (perm, spans)
+    with spans a list of (s0, s1, r0, r1, admissible), half-open ranges of
+    positions in the order perm."""
+    L = _lib.load()
+    c = np.ascontiguousarray(np.asarray(centres, dtype=np.float64).reshape(-1, 3))
+    N = c.shape[0]
+    h = C.c_void_p()
+    _lib.check(L.qdfn_hstruct_build(C.byref(h), N, C.c_void_p(c.ctypes.data), int(leaf), float(eta)))
+    try:
+        nb = C.c_int64()
+        _lib.check(L.qdfn_hstruct_sizes(h, C.byref(nb), None))
+        perm = np.zeros(N, dtype=np.int64)
+        ranges = np.zeros((nb.value, 4), dtype=np.int64)
+        adm = np.zeros(nb.value, dtype=np.int32)
+        _lib.check(L.qdfn_hstruct_get(h, C.c_void_p(perm.ctypes.data), C.c_void_p(ranges.ctypes.data),
+                                      C.c_void_p(adm.ctypes.data)))
+    finally:
+        L.qdfn_hstruct_destroy(h)
+    spans = [(int(a), int(b) + 1, int(c_), int(d) + 1, bool(m)) for (a, b, c_, d), m in zip(ranges, adm)]
+    return perm, spans
+
+
+def host_partition(centres, leaf=64, eta=2.0):
+    """The same (perm, spans) from the host principal-axis tree (ClusterTree)
+    and block_partition."""
+    tree = ClusterTree(np.asarray(centres), leaf=leaf)
+    spans = [(tree.starts[s], tree.ends[s], tree.starts[t], tree.ends[t], adm)
+             for (s, t, adm) in block_partition(tree, eta)]
+    return tree.perm, spans
+
+
+def partition(centres, leaf, eta, tree):
+    if tree == "device":
+        return device_partition(centres, leaf, eta)
+    if tree == "pca":
+        return host_partition(centres, leaf, eta)
+    raise ValueError("tree must be 'device' or 'pca'")
 
 
 def aca(block, tol, max_rank=None):
@@ -191,20 +234,17 @@ class HMatrix:
         return Ks, Kn
 
 
-def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, device="cuda"):
+def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, device="cuda", tree="pca"):
     """Build the H-matrix of a rectangular-patch system (records n x 8).
+    tree: "pca" (host principal-axis bisection) or "device" (qdfn_hstruct_build).
     Returns (HMatrix, perm): block ranges index the permuted ordering
     records[perm]."""
     import torch
     from . import assemble
-    tree = ClusterTree(np.asarray(records)[:, :3] * np.array([1.0, 1.0, -1.0]), leaf=leaf)
-    perm = tree.perm
+    perm, spans = partition(np.asarray(records)[:, :3] * np.array([1.0, 1.0, -1.0]), leaf, eta, tree)
     rec = torch.tensor(np.ascontiguousarray(np.asarray(records)[perm]), dtype=torch.float64, device=device)
-    blocks = block_partition(tree, eta)
     ranges, ds, us, vs, dn, un, vn = [], [], [], [], [], [], []
-    for (s, t, adm) in blocks:
-        s0, s1 = tree.starts[s], tree.ends[s]
-        r0, r1 = tree.starts[t], tree.ends[t]
+    for (s0, s1, r0, r1, adm) in spans:
         ns, nr = s1 - s0, r1 - r0
         Ks = torch.empty((ns, nr), dtype=torch.float64, device=device)
         Kn = torch.empty((ns, nr), dtype=torch.float64, device=device)
@@ -225,7 +265,7 @@ def build_rect(records, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6, devi
 
 
 def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf=64, eta=2.0, tol=1e-6,
-              device="cuda", chunk=1 << 24):
+              device="cuda", chunk=1 << 24, tree="pca"):
     """Build the H-matrix of a triangular-patch system (TDstressHS kernels,
     StiffnessMatrix_ByParts_Calculation_Tri, scripts/Functions_BuildInputFile.jl:551-594,
     in the block structure HmatBuild_T builds at :643-723).  Entries are
@@ -233,12 +273,12 @@ def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf
     near-field blocks whole, in batches of `chunk` entries, and the admissible
     blocks only where batched ACA asks for them (one row and one column per
     block and iteration, every block in the same launches) -- no admissible
-    block is ever formed whole.  Returns (HMatrix, perm): block ranges index
-    the permuted ordering (every per-patch array [perm])."""
+    block is ever formed whole.  tree: "pca" (host principal-axis bisection)
+    or "device" (qdfn_hstruct_build).  Returns (HMatrix, perm): block ranges
+    index the permuted ordering (every per-patch array [perm])."""
     import torch
     from . import assemble
-    tree = ClusterTree(np.asarray(centre), leaf=leaf)
-    perm = tree.perm
+    perm, pspans = partition(np.asarray(centre), leaf, eta, tree)
     dv = lambda a: torch.tensor(np.ascontiguousarray(np.asarray(a)[perm]), dtype=torch.float64,
                                 device=device)
     p1, p2, p3, rk, cen, nh, sh = (dv(a) for a in (P1, P2, P3, rake, centre, nhat, shat))
@@ -275,11 +315,10 @@ def build_tri(P1, P2, P3, rake, centre, nhat, shat, shear_modulus, poisson, leaf
                 off += n
         return res
 
-    parts = block_partition(tree, eta)
-    spans = [(tree.starts[s], tree.ends[s], tree.starts[t], tree.ends[t]) for (s, t, _) in parts]
-    near = [k for k, (_, _, adm) in enumerate(parts) if not adm]
-    far = [k for k, (_, _, adm) in enumerate(parts) if adm]
-    nb = len(parts)
+    spans = [sp[:4] for sp in pspans]
+    near = [k for k, sp in enumerate(pspans) if not sp[4]]
+    far = [k for k, sp in enumerate(pspans) if sp[4]]
+    nb = len(pspans)
     ds, us, vs, dn, un, vn = ([None] * nb for _ in range(6))
     for k, (Bs, Bn) in zip(near, dense_blocks([spans[k] for k in near])):
         ds[k], dn[k] = Bs, Bn
