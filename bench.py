@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--tri-edge", type=float, default=80.0,
                     help="tri_h: triangle edge in m (80: ~50,000 triangles; 160: ~12,500)")
+    ap.add_argument("--tree", default="pca", choices=["pca", "device"],
+                    help="tri_h: H-matrix cluster tree and partition -- host principal-axis bisection, or built "
+                         "on the device (qdfn_hstruct_build)")
     ap.add_argument("--cpu-members", type=int, default=4,
                     help="ensemble members (at size quantiles) in the CPU oracle sample and the reference arm")
     ap.add_argument("--plain-members", type=int, default=16,
@@ -1067,7 +1070,8 @@ def run_tri_h(args):
     P1, P2, P3, un, _, _, us = geometry.rot_verts_unit_vectors_abi(seg, seg[:, 9])
     cen = (P1 + P2 + P3) / 3
     t0 = time.perf_counter()
-    H, perm = hmatrix.build_tri(P1, P2, P3, seg[:, 9], cen, un, us, net["G"], net["nu"], leaf=64, eta=2.0, tol=1e-6)
+    H, perm = hmatrix.build_tri(P1, P2, P3, seg[:, 9], cen, un, us, net["G"], net["nu"], leaf=64, eta=2.0, tol=1e-6,
+                                tree=args.tree)
     build_s = time.perf_counter() - t0
     N = net["N"]
     kdiag = np.zeros(N)
@@ -1136,7 +1140,7 @@ def run_tri_h(args):
                        "patches": N, "blocks": int(H.nblocks), "low_rank_blocks": nlr,
                        "max_rank": int(max(ranks)) if ranks else 0, "mean_rank": float(np.mean(ranks)) if ranks else 0,
                        "stored_entries": int(stored), "compression_vs_dense": float(stored / (2.0 * N * N)),
-                       "h_build_s": build_s},
+                       "h_build_s": build_s, "tree": args.tree},
             "gpu_launches": 1,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,

@@ -162,10 +162,11 @@ int qdfn_set_dense_dev(qdfn_ctx* ctx, const double* Ks, const double* Kn, int64_
 /* The cluster tree and block partition of an H-matrix operator, built on the
  * GPU (replaces GroupAndSort_AllLevel / BuildHierarchy,
  * scripts/Functions_Hmatrix.jl:1-212, whose k-means tree is randomly
- * initialised).  centres: host [N][3] element centres.  The elements are
- * ordered by the Morton key of their centre (21 bits per axis in the centres'
- * bounding box; ties by index), every node of more than `leaf` elements splits
- * its range in halves, and a (receiver node, source node) pair is a low-rank
+ * initialised).  centres: host [N][3] element centres.  Level by level, every
+ * node of more than `leaf` elements orders its elements along the longest
+ * axis of its box (ties: lower axis, then lower element index) and splits its
+ * range in halves (a k-d tree of median splits), and a (receiver node, source
+ * node) pair is a low-rank
  * block when its boxes are apart (dist > 0) and max(diameter) <= eta * dist, a
  * dense block when both nodes are leaves, and is split otherwise.
  * qdfn_hstruct_get: perm [N] (element at each position), ranges [n_blocks][4]

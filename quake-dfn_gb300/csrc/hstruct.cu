@@ -4,14 +4,15 @@
 // scripts/Functions_Hmatrix.jl:1-212), whose random initialisation makes its
 // trees irreproducible.
 //
-//  1. Morton order: the centres are quantised to 21 bits per axis inside their
-//     bounding box and their bits interleaved (x lowest); the (key, index)
-//     pairs are sorted by a bitonic network (one launch per merge stage), so
-//     nearby centres are nearby in the order.
-//  2. Tree: every node of more than `leaf` elements splits its range of the
-//     order in two halves (the first half the smaller or equal one); node
-//     boxes are the exact min/max of the centres of their leaves, reduced
-//     bottom-up level by level.
+//  1. Tree: level by level, every node of more than `leaf` elements orders
+//     its elements by their centre's coordinate along the longest axis of the
+//     node's box (ties: the lower axis; equal coordinates: the lower element
+//     index) and splits its range in two halves (the first floor(n / 2)): a
+//     k-d tree of median splits.  All nodes of a level are ordered by ONE
+//     bitonic sort of (node start, coordinate key, element) over the whole
+//     order (one launch per merge stage); elements of nodes that do not split
+//     keep their places (their key is their position).
+//  2. Boxes: the exact min/max of each node's centres, one warp per node.
 //  3. Partition: a frontier of (receiver node, source node) pairs, one thread
 //     each per launch: admissible when dist > 0 and max(diam) <= eta * dist
 //     (box diagonal, box-to-box distance) -> low-rank block; both leaves -> dense block;
@@ -43,79 +44,20 @@ struct qdfn_hstruct {
 namespace qdfn {
 namespace {
 
-constexpr unsigned kQuant = 2097151u;   // 2^21 - 1
-
 __device__ __forceinline__ unsigned long long ord_key_d(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     return b ^ ((unsigned long long)((long long)b >> 63) | 0x8000000000000000ull);
 }
 
-// bounding box of all centres: keys[0..2] min, keys[3..5] max (order-preserving keys)
-__global__ void k_bbox(int64_t N, const double* __restrict__ c, unsigned long long* keys) {
-    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-        for (int a = 0; a < 3; ++a) {
-            const unsigned long long k = ord_key_d(c[i * 3 + a]);
-            mn[a] = k < mn[a] ? k : mn[a];
-            mx[a] = k > mx[a] ? k : mx[a];
-        }
-    for (int a = 0; a < 3; ++a) {
-        atomicMin(keys + a, mn[a]);
-        atomicMax(keys + 3 + a, mx[a]);
-    }
-}
-
-__device__ __forceinline__ unsigned long long spread3(unsigned v) {   // 21 bits -> every third bit
-    unsigned long long x = v & 0x1fffffull;
-    x = (x | (x << 32)) & 0x1f00000000ffffull;
-    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
-    x = (x | (x << 8)) & 0x100f00f00f00f00full;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
-    return x;
-}
-
-__global__ void k_morton(int64_t N, int64_t npad, const double* __restrict__ c, const double* __restrict__ lo,
-                         const double* __restrict__ scale, unsigned long long* key, long long* idx) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npad) return;
-    if (i >= N) {   // padding sorts last
-        key[i] = ~0ull;
-        idx[i] = 0x7fffffffffffffffll;
-        return;
-    }
-    unsigned q[3];
-    for (int a = 0; a < 3; ++a) {
-        const double t = (c[i * 3 + a] - lo[a]) * scale[a];   // >= 0, <= 2^21 - 1 up to rounding
-        q[a] = t >= (double)kQuant ? kQuant : (unsigned)t;
-    }
-    key[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
-    idx[i] = (long long)i;
-}
-
-// one compare-exchange stage of the bitonic network over (key, idx)
-__global__ void k_bitonic(int64_t npad, unsigned long long* key, long long* idx, int64_t j, int64_t k) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npad) return;
-    const int64_t l = i ^ j;
-    if (l <= i) return;
-    const bool up = (i & k) == 0;
-    const unsigned long long ka = key[i], kb = key[l];
-    const long long ia = idx[i], ib = idx[l];
-    const bool greater = ka > kb || (ka == kb && ia > ib);
-    if (greater == up) {
-        key[i] = kb; key[l] = ka;
-        idx[i] = ib; idx[l] = ia;
-    }
-}
-
-// leaf boxes: one warp per leaf node, exact min/max over its centres
-__global__ void k_leaf_boxes(int nleaf, const int* __restrict__ leaves, const long long* __restrict__ nstart,
-                             const long long* __restrict__ nend, const long long* __restrict__ order,
-                             const double* __restrict__ c, double* lo, double* hi) {
+// boxes of the nodes of one level: one warp per node, exact min/max of its
+// centres; the split axis (longest extent, the lower axis on ties) is written
+// at the node's start position for splitting nodes, -1 for the others
+__global__ void k_level_boxes(int n, const int* __restrict__ nodes, const long long* __restrict__ nstart,
+                              const long long* __restrict__ nend, const long long* __restrict__ order,
+                              const double* __restrict__ c, int leaf, double* lo, double* hi, int* axis_at) {
     const int w = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (w >= nleaf) return;
-    const int node = leaves[w];
+    if (w >= n) return;
+    const int node = nodes[w];
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (long long p = nstart[node] + lane; p < nend[node]; p += 32) {
         const long long e = order[p];
@@ -129,24 +71,67 @@ __global__ void k_leaf_boxes(int nleaf, const int* __restrict__ leaves, const lo
             mn[a] = fmin(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
             mx[a] = fmax(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
         }
-    if (lane == 0)
+    if (lane == 0) {
         for (int a = 0; a < 3; ++a) {
             lo[node * 3 + a] = mn[a];
             hi[node * 3 + a] = mx[a];
         }
+        int ax = 0;
+        if (mx[1] - mn[1] > mx[ax] - mn[ax]) ax = 1;
+        if (mx[2] - mn[2] > mx[ax] - mn[ax]) ax = 2;
+        axis_at[nstart[node]] = (nend[node] - nstart[node] > leaf) ? ax : -1;
+    }
 }
 
-// internal node boxes of one level from their children's
-__global__ void k_parent_boxes(int n, const int* __restrict__ nodes, const int2* __restrict__ child, double* lo,
-                               double* hi) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int v = nodes[t];
-    const int2 ch = child[v];
-    for (int a = 0; a < 3; ++a) {
-        lo[v * 3 + a] = fmin(lo[ch.x * 3 + a], lo[ch.y * 3 + a]);
-        hi[v * 3 + a] = fmax(hi[ch.x * 3 + a], hi[ch.y * 3 + a]);
+// sort keys of one level: (start of the position's node, coordinate key or
+// the position itself, element)
+__global__ void k_level_keys(int64_t N, int64_t npad, const long long* __restrict__ seg,
+                             const int* __restrict__ axis_at, const long long* __restrict__ order,
+                             const double* __restrict__ c, long long* k1, unsigned long long* k2, long long* idx) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npad) return;
+    if (p >= N) {   // padding sorts last
+        k1[p] = 0x7fffffffffffffffll;
+        k2[p] = ~0ull;
+        idx[p] = 0x7fffffffffffffffll;
+        return;
     }
+    const long long s = seg[p], e = order[p];
+    const int ax = axis_at[s];
+    k1[p] = s;
+    k2[p] = ax >= 0 ? ord_key_d(c[e * 3 + ax] + 0.0) : (unsigned long long)p;   // (+0.0: -0 and 0 compare equal)
+    idx[p] = e;
+}
+
+// one compare-exchange stage of the bitonic network over (k1, k2, idx)
+__global__ void k_bitonic3(int64_t npad, long long* k1, unsigned long long* k2, long long* idx, int64_t j,
+                           int64_t k) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    const int64_t l = i ^ j;
+    if (l <= i) return;
+    const bool up = (i & k) == 0;
+    const long long a1 = k1[i], b1 = k1[l];
+    const unsigned long long a2 = k2[i], b2 = k2[l];
+    const long long a3 = idx[i], b3 = idx[l];
+    const bool greater = a1 != b1 ? a1 > b1 : (a2 != b2 ? a2 > b2 : a3 > b3);
+    if (greater == up) {
+        k1[i] = b1; k1[l] = a1;
+        k2[i] = b2; k2[l] = a2;
+        idx[i] = b3; idx[l] = a3;
+    }
+}
+
+// the children's segments of the splitting nodes of a level: one warp per node
+__global__ void k_level_split(int n, const int* __restrict__ nodes, const long long* __restrict__ nstart,
+                              const long long* __restrict__ nend, int leaf, long long* seg) {
+    const int w = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const int node = nodes[w];
+    const long long s = nstart[node], e = nend[node];
+    if (e - s <= leaf) return;
+    const long long h = s + (e - s) / 2;
+    for (long long p = s + lane; p < e; p += 32) seg[p] = p < h ? s : h;
 }
 
 __device__ __forceinline__ double norm3(double x, double y, double z) { return sqrt((x * x + y * y) + z * z); }
@@ -225,63 +210,54 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     const int nn = (int)nstart.size();
     int64_t npad = 1;
     while (npad < N) npad <<= 1;
-    DBuf<double> dc, dlo, dhi, dbox;
-    DBuf<unsigned long long> dkeys, dkey;
-    DBuf<long long> didx, dns, dne;
+    int maxlev = 0;
+    for (int v = 0; v < nn; ++v) maxlev = std::max(maxlev, level[v]);
+    DBuf<double> dc, dlo, dhi;
+    DBuf<unsigned long long> dk2;
+    DBuf<long long> dk1, didx, dorder, dseg, dns, dne;
+    DBuf<int> daxis, dnodes;
     DBuf<int2> dchild;
     int rc;
-    if ((rc = dc.alloc(3 * N)) || (rc = dkeys.alloc(6)) || (rc = dkey.alloc(npad)) || (rc = didx.alloc(npad)) ||
-        (rc = dbox.alloc(6)) || (rc = dlo.alloc(3 * (size_t)nn)) || (rc = dhi.alloc(3 * (size_t)nn)) ||
-        (rc = dns.alloc(nn)) || (rc = dne.alloc(nn)) || (rc = dchild.alloc(nn)))
+    if ((rc = dc.alloc(3 * N)) || (rc = dk1.alloc(npad)) || (rc = dk2.alloc(npad)) || (rc = didx.alloc(npad)) ||
+        (rc = dorder.alloc(N)) || (rc = dseg.alloc(N)) || (rc = daxis.alloc(N)) || (rc = dnodes.alloc(nn)) ||
+        (rc = dlo.alloc(3 * (size_t)nn)) || (rc = dhi.alloc(3 * (size_t)nn)) || (rc = dns.alloc(nn)) ||
+        (rc = dne.alloc(nn)) || (rc = dchild.alloc(nn)))
         return rc;
     QDFN_CUDA(cudaMemcpy(dc.p, centres, 3 * N * sizeof(double), cudaMemcpyHostToDevice));
-    const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull};
-    QDFN_CUDA(cudaMemcpy(dkeys.p, init, sizeof(init), cudaMemcpyHostToDevice));
-    k_bbox<<<(unsigned)std::min<int64_t>((N + 255) / 256, 1024), 256>>>(N, dc.p, dkeys.p);
-    QDFN_CUDA(cudaGetLastError());
-    unsigned long long keys[6];
-    QDFN_CUDA(cudaMemcpy(keys, dkeys.p, sizeof(keys), cudaMemcpyDeviceToHost));
-    double box[6];   // lo[3], scale[3]
-    for (int a = 0; a < 3; ++a) {
-        auto val = [](unsigned long long k) {
-            const unsigned long long b = (k & 0x8000000000000000ull) ? (k ^ 0x8000000000000000ull) : ~k;
-            double d;
-            std::memcpy(&d, &b, 8);
-            return d;
-        };
-        const double lo = val(keys[a]), hi = val(keys[3 + a]);
-        box[a] = lo;
-        box[3 + a] = hi > lo ? (double)kQuant / (hi - lo) : 0.0;
+    {
+        std::vector<long long> iota(N);
+        for (int64_t i = 0; i < N; ++i) iota[i] = i;
+        QDFN_CUDA(cudaMemcpy(dorder.p, iota.data(), N * sizeof(long long), cudaMemcpyHostToDevice));
     }
-    QDFN_CUDA(cudaMemcpy(dbox.p, box, sizeof(box), cudaMemcpyHostToDevice));
-    k_morton<<<(unsigned)((npad + 255) / 256), 256>>>(N, npad, dc.p, dbox.p, dbox.p + 3, dkey.p, didx.p);
-    QDFN_CUDA(cudaGetLastError());
-    for (int64_t k = 2; k <= npad; k <<= 1)
-        for (int64_t j = k >> 1; j > 0; j >>= 1) k_bitonic<<<(unsigned)((npad + 255) / 256), 256>>>(npad, dkey.p, didx.p, j, k);
-    QDFN_CUDA(cudaGetLastError());
-    // node boxes, leaves first, then the levels bottom-up
+    QDFN_CUDA(cudaMemset(dseg.p, 0, N * sizeof(long long)));
     QDFN_CUDA(cudaMemcpy(dns.p, nstart.data(), nn * sizeof(long long), cudaMemcpyHostToDevice));
     QDFN_CUDA(cudaMemcpy(dne.p, nend.data(), nn * sizeof(long long), cudaMemcpyHostToDevice));
     QDFN_CUDA(cudaMemcpy(dchild.p, child.data(), nn * sizeof(int2), cudaMemcpyHostToDevice));
-    std::vector<int> leaves;
-    int maxlev = 0;
-    for (int v = 0; v < nn; ++v) {
-        if (child[v].x < 0) leaves.push_back(v);
-        maxlev = std::max(maxlev, level[v]);
-    }
-    DBuf<int> dnodes;
-    if ((rc = dnodes.alloc(nn))) return rc;
-    QDFN_CUDA(cudaMemcpy(dnodes.p, leaves.data(), leaves.size() * sizeof(int), cudaMemcpyHostToDevice));
-    k_leaf_boxes<<<(unsigned)((leaves.size() * 32 + 255) / 256), 256>>>((int)leaves.size(), dnodes.p, dns.p, dne.p,
-                                                                         didx.p, dc.p, dlo.p, dhi.p);
-    QDFN_CUDA(cudaGetLastError());
-    for (int l = maxlev - 1; l >= 0; --l) {
+    // level by level: the boxes, then one sort orders every splitting node
+    // along its axis, then the children's segments
+    for (int l = 0; l <= maxlev; ++l) {
         std::vector<int> lv;
+        bool splits = false;
         for (int v = 0; v < nn; ++v)
-            if (level[v] == l && child[v].x >= 0) lv.push_back(v);
-        if (lv.empty()) continue;
+            if (level[v] == l) {
+                lv.push_back(v);
+                splits = splits || child[v].x >= 0;
+            }
         QDFN_CUDA(cudaMemcpy(dnodes.p, lv.data(), lv.size() * sizeof(int), cudaMemcpyHostToDevice));
-        k_parent_boxes<<<(unsigned)((lv.size() + 255) / 256), 256>>>((int)lv.size(), dnodes.p, dchild.p, dlo.p, dhi.p);
+        const unsigned wb = (unsigned)((lv.size() * 32 + 255) / 256);
+        k_level_boxes<<<wb, 256>>>((int)lv.size(), dnodes.p, dns.p, dne.p, dorder.p, dc.p, leaf, dlo.p, dhi.p,
+                                    daxis.p);
+        QDFN_CUDA(cudaGetLastError());
+        if (!splits) continue;
+        k_level_keys<<<(unsigned)((npad + 255) / 256), 256>>>(N, npad, dseg.p, daxis.p, dorder.p, dc.p, dk1.p,
+                                                              dk2.p, didx.p);
+        QDFN_CUDA(cudaGetLastError());
+        for (int64_t k = 2; k <= npad; k <<= 1)
+            for (int64_t j = k >> 1; j > 0; j >>= 1)
+                k_bitonic3<<<(unsigned)((npad + 255) / 256), 256>>>(npad, dk1.p, dk2.p, didx.p, j, k);
+        QDFN_CUDA(cudaGetLastError());
+        QDFN_CUDA(cudaMemcpy(dorder.p, didx.p, N * sizeof(long long), cudaMemcpyDeviceToDevice));
+        k_level_split<<<wb, 256>>>((int)lv.size(), dnodes.p, dns.p, dne.p, leaf, dseg.p);
         QDFN_CUDA(cudaGetLastError());
     }
     // partition by frontier rounds; buffers grow and the round is redone when a count overflows
@@ -333,7 +309,7 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     h->perm.resize(N);
     {
         std::vector<long long> order(N);
-        QDFN_CUDA(cudaMemcpy(order.data(), didx.p, N * sizeof(long long), cudaMemcpyDeviceToHost));
+        QDFN_CUDA(cudaMemcpy(order.data(), dorder.p, N * sizeof(long long), cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < N; ++i) h->perm[i] = order[i];
     }
     // a fixed block order: by receiver start, then source start

@@ -95,8 +95,8 @@ def block_partition(tree, eta=2.0):
 
 def device_partition(centres, leaf=64, eta=2.0):
     """The cluster tree and block partition built on the GPU
-    (qdfn_hstruct_build: Morton order of the centres, halving tree,
-    admissibility dist > 0 and max(diam) <= eta * dist).  Returns (perm, spans)
+    (qdfn_hstruct_build: k-d tree of median splits along each node's longest
+    box axis, admissibility dist > 0 and max(diam) <= eta * dist).  Returns (perm, spans)
     with spans a list of (s0, s1, r0, r1, admissible), half-open ranges of
     positions in the order perm."""
     L = _lib.load()

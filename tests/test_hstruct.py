@@ -1,14 +1,13 @@
-"""The H-matrix structure built on the device (qdfn_hstruct_*: Morton order of
-the element centres, halving cluster tree, block partition) against a host
-restatement of the same rules -- the permutation and the block list must be
-equal, element for element -- plus the partition's invariants and an
-operator compressed on it.
+"""The H-matrix structure built on the device (qdfn_hstruct_*: k-d cluster
+tree of median splits, block partition) against a host restatement of the
+same rules -- the permutation and the block list must be equal, element for
+element -- plus the partition's invariants and an operator compressed on it.
 
-The rules restated here: centres quantised to 21 bits per axis inside their
-bounding box (t = (c - lo) * (2^21 - 1) / (hi - lo), truncated, clamped),
-bits interleaved x-lowest, sorted by (key, index); every node of more than
-`leaf` elements splits its range into halves (first half = floor(n / 2));
-boxes are the min/max of a node's centres; a (receiver, source) node pair is
+The rules restated here: level by level, every node of more than `leaf`
+elements orders its elements by the centre coordinate along the longest axis
+of its box (the lower axis on ties; equal coordinates by element index) and
+splits its range into halves (first half = floor(n / 2)); boxes are the
+min/max of a node's centres; a (receiver, source) node pair is
 low-rank when dist > 0 and max(diam) <= eta * dist (diam = box diagonal, dist
 = box-to-box distance, each sqrt((x*x + y*y) + z*z)), dense when both are
 leaves, else split (a leaf stands in for its children).  These replace the
@@ -21,36 +20,32 @@ pytestmark = pytest.mark.gpu
 G, NU = 32e9, 0.25
 
 
-def _morton_perm(c):
-    lo, hi = c.min(axis=0), c.max(axis=0)
-    span = hi - lo
-    scale = np.where(span > 0, 2097151.0 / np.where(span > 0, span, 1.0), 0.0)
-    t = (c - lo) * scale
-    q = np.where(t >= 2097151.0, 2097151.0, np.floor(t)).astype(np.uint64)
-    key = np.zeros(c.shape[0], dtype=np.uint64)
-    for b in range(21):
-        for a in range(3):
-            key |= ((q[:, a] >> np.uint64(b)) & np.uint64(1)) << np.uint64(3 * b + a)
-    return np.lexsort((np.arange(c.shape[0]), key))
-
-
 def _host_structure(c, leaf, eta):
-    perm = _morton_perm(c)
-    pts = c[perm]
-    start, end, child = [0], [c.shape[0]], []
+    N = c.shape[0]
+    start, end, child, level = [0], [N], [], [0]
     v = 0
-    while v < len(start):
+    while v < len(start):   # the tree's shape: level order, halving
         n = end[v] - start[v]
         if n > leaf:
             h = n // 2
             child.append((len(start), len(start) + 1))
             start += [start[v], start[v] + h]
             end += [start[v] + h, end[v]]
+            level += [level[v] + 1, level[v] + 1]
         else:
             child.append(None)
         v += 1
-    lo = [pts[a:b].min(axis=0) for a, b in zip(start, end)]
-    hi = [pts[a:b].max(axis=0) for a, b in zip(start, end)]
+    order = np.arange(N)
+    lo, hi = [None] * len(start), [None] * len(start)
+    for lv in range(max(level) + 1):   # boxes, then each splitting node sorted along its longest axis
+        for v in (k for k in range(len(start)) if level[k] == lv):
+            pts = c[order[start[v]:end[v]]]
+            lo[v], hi[v] = pts.min(axis=0), pts.max(axis=0)
+            if child[v] is not None:
+                ax = int(np.argmax(hi[v] - lo[v]))
+                seg = order[start[v]:end[v]]
+                order[start[v]:end[v]] = seg[np.lexsort((seg, pts[:, ax] + 0.0))]
+    perm = order
     norm = lambda x: float(np.sqrt((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2]))
     blocks = []
     stack = [(0, 0)]
