@@ -191,6 +191,7 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     if (!(eta > 0) || !std::isfinite(eta)) return fail(QDFN_ERR_INVALID, "eta must be positive");
     for (int64_t i = 0; i < 3 * N; ++i)
         if (!std::isfinite(centres[i])) return fail(QDFN_ERR_INVALID, "centres must be finite");
+    if (N / leaf > ((int64_t)1 << 27)) return fail(QDFN_ERR_INVALID, "too many tree nodes (raise leaf)");
     // the tree's shape depends on N and leaf only: level order, halving
     std::vector<long long> nstart{0}, nend{N};
     std::vector<int2> child;
@@ -207,6 +208,7 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
             child.push_back(make_int2(-1, -1));
         }
     }
+    if (nstart.size() >= (size_t)1 << 30) return fail(QDFN_ERR_INVALID, "too many tree nodes (raise leaf)");
     const int nn = (int)nstart.size();
     int64_t npad = 1;
     while (npad < N) npad <<= 1;
@@ -263,7 +265,7 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     // partition by frontier rounds; buffers grow and the round is redone when a count overflows
     std::vector<int4> blocks;
     {
-        unsigned cap_f = 1u << 16, cap_b = (unsigned)std::min<int64_t>((int64_t)1 << 30, 256 * (int64_t)nn + 1024);
+        unsigned cap_f = 1u << 16, cap_b = (unsigned)std::min<int64_t>((int64_t)1 << 30, 64 * (int64_t)nn + 1024);
         DBuf<int2> fa, fb;
         DBuf<int4> db;
         DBuf<unsigned> dcnt;   // [0] next frontier, [1] blocks
