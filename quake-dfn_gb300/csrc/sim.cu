@@ -1507,7 +1507,7 @@ extern "C" int qdfn_apply_operator(qdfn_ctx* c, const double* D, double* tld, do
         QDFN_CUDA(cudaGetLastError());
         b<<<c->nblocks, kSimThreads, c->smem>>>(p);
         QDFN_CUDA(cudaGetLastError());
-        rows<<<(unsigned)((tot + 255) / 256), 256>>>(p);
+        rows<<<(unsigned)((tot + 31) / 32), 256>>>(p);   // 32 rows per block
         QDFN_CUDA(cudaGetLastError());
     } else {
         QDFN_CUDA(cudaMemset(c->tile_ctr, 0, sizeof(unsigned long long)));

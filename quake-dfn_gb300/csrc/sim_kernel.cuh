@@ -1226,15 +1226,10 @@ __device__ __forceinline__ void sim_run(const SimParams& p, int64_t nsteps, cons
             // the row's products: formed here in a step's first pass (and kept
             // in registers for this solve), read back in a retry pass
             double tld_q = 0.0, knd_q = 0.0;
+            // (H-matrix: a step's first pass forms the products block-wide
+            // before its solves, hmat::row_sums_block, so every solve reads them)
             if (first) {
-                if constexpr (HM) {
-                    // main_H :241-248: H_load (0 - D) ./ -K_Self and H_n D
-                    const double ss = hmat::row_sum<R>(p.h, 0, N, i, r);
-                    tld_q = (-ss) / -p.kself[i];
-                    knd_q = hmat::row_sum<R>(p.h, 1, N, i, r);
-                    p.tld[q] = tld_q;
-                    p.knd[q] = knd_q;
-                } else {
+                if constexpr (!HM) {
                     double ss, sn;
                     if (pair) {   // the even lane sums the shear partials, the odd lane the normal ones
                         const unsigned pm = 3u << (threadIdx.x & 30);
@@ -1855,14 +1850,13 @@ __global__ void __launch_bounds__(kSimThreads, 1) k_hmat_b(SimParams p) {
     extern __shared__ unsigned char smem_raw[];
     hmat::pass_b<X, R>(p.h, p.D, p.N, 0ull, kWaitLimitNs, p.gerr);   // pass A ran in the launch before
 }
+// receiver-row sums of the operator-only H product: 32 rows per 256-thread
+// block (eight threads per row: four per matrix)
 template <int R>
 __global__ void k_hmat_rows(SimParams p) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= (int64_t)R * p.N) return;
-    const int r = (int)(q / p.N);
-    const int64_t i = q - (int64_t)r * p.N;
-    p.tld[q] = (-hmat::row_sum<R>(p.h, 0, p.N, i, r)) / -p.kself[i];
-    p.knd[q] = hmat::row_sum<R>(p.h, 1, p.N, i, r);
+    const int64_t q0 = (int64_t)blockIdx.x * (blockDim.x / 8);
+    const int64_t q1 = min((int64_t)R * p.N, q0 + (int64_t)(blockDim.x / 8));
+    hmat::row_sums_block<R>(p.h, p.N, p.kself, p.tld, p.knd, q0, q1);
 }
 
 template <bool kPairs>
