@@ -26,6 +26,33 @@ def test_sm_shares_are_proportional_and_fit():
         sm_shares([1.0, 0.0], 152)                   # costs must be positive
 
 
+def test_state_record_layout_round_trips():
+    """The ensemble state record (qdfn_ensemble_set/get_state_all's host
+    buffer): member after member [6][n_inst][N] doubles, then T, dt and step
+    [n_inst] as 8-byte words -- packed and unpacked on the host, no GPU."""
+    import types
+    from qdfn import ensemble, simulate
+    rng = np.random.default_rng(0)
+    sims = [types.SimpleNamespace(n_inst=R, N=N) for R, N in ((4, 7), (1, 3), (2, 5))]
+    words = sum(6 * m.n_inst * m.N + 3 * m.n_inst for m in sims)
+    ens = types.SimpleNamespace(members=sims, state_words=lambda: words)
+    states = [[dict({k: rng.normal(size=m.N) for k in simulate.Simulation.STATE_FIELDS},
+                    T=float(rng.uniform()), dt=float(rng.uniform()), step=int(rng.integers(0, 1 << 40)))
+               for _ in range(m.n_inst)] for m in sims]
+    buf = ensemble.Ensemble.pack_states(ens, states)
+    assert buf.shape == (words,)
+    # member 1 starts after member 0's 6*4*7 + 3*4 words; its V is first, its step last
+    o1 = 6 * 4 * 7 + 12
+    assert np.array_equal(buf[o1:o1 + 3], states[1][0]["V"])
+    assert buf[o1 + 18 + 2:o1 + 18 + 3].view(np.int64)[0] == states[1][0]["step"]
+    back = ensemble.Ensemble.unpack_states(ens, buf)
+    for a, b in zip(back, states):
+        for x, y in zip(a, b):
+            assert x["T"] == y["T"] and x["dt"] == y["dt"] and x["step"] == y["step"]
+            for k in simulate.Simulation.STATE_FIELDS:
+                assert np.array_equal(x[k], y[k])
+
+
 def _member(seed, R, n_faults=4, patch=400.0, length=(1200.0, 2400.0)):
     """One geometry with R friction draws: the member dict and what its oracle
     runs need."""
