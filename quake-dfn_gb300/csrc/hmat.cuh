@@ -344,29 +344,6 @@ __device__ bool pass_b(const Ops& h, const double* __restrict__ D, int64_t N, un
     return true;
 }
 
-// sum of the partials of receiver row i (side 0 shear, 1 normal), block order;
-// eight slot indices and then eight partials are loaded before they are added
-// (in the same order), so a row's loads overlap instead of forming a chain
-template <int R>
-__device__ __forceinline__ double row_sum(const Ops& h, int side, int64_t N, int64_t i, int r) {
-    const int64_t* rp = h.rowptr + side * (N + 1);
-    const int64_t q1 = __ldg(rp + i + 1);
-    int64_t q = __ldg(rp + i);
-    double s = 0.0;
-    for (; q + 8 <= q1; q += 8) {
-        int64_t sl[8];
-        double v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) sl[u] = __ldg(h.rowslot + q + u);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = __ldcg(h.part + sl[u] * R + r);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
-    }
-    for (; q < q1; ++q) s += __ldcg(h.part + __ldg(h.rowslot + q) * R + r);
-    return s;
-}
-
 // The products of a block's solve items q0..q1-1 (q = r N + i) for a step's
 // first solve pass, by the whole block before its solves: four threads per
 // (item, matrix), each summing every fourth partial of the row in block
