@@ -21,9 +21,11 @@
 //                                     lane per row (two rows), the x or t
 //                                     values held by the lanes and broadcast
 //                                     by shuffles, coalesced loads of D^T / U^T
-// and every receiver row then sums its partials in block order (a fixed
-// order, so results are reproducible run to run).  Tasks are listed largest
-// first and dealt out to the warps in snake order, which spreads the long ones.
+// and every receiver row then sums its partials (row_sums_block: four threads
+// per row and matrix, each over every fourth partial in block order, combined
+// in a fixed order, so results are reproducible run to run).  Tasks are listed
+// largest first and dealt out to the warps in snake order, which spreads the
+// long ones.
 #pragma once
 #include "qdfn_internal.h"
 
