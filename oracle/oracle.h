@@ -1,8 +1,8 @@
 // CPU FP64 oracle of the Quake-DFN earthquake-cycle hot path.
 //
-// TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the bench's CPU
-// baseline leg use it as the checker.  The shipped CUDA library never includes,
-// links or calls anything here.
+// TEST INFRASTRUCTURE ONLY: the tests and the smoke check compare the GPU
+// results with it, and the bench's CPU baseline leg times it.  The shipped
+// CUDA library never includes, links or calls anything here.
 //
 // PARITY STATUS: the reference (pure Julia) ships no tests, golden vectors or
 // fixtures, and Julia is not available to run it, so this restatement is

@@ -1,8 +1,9 @@
 """ctypes binding of the CPU FP64 oracle (liboracle.so).
 
-TEST INFRASTRUCTURE ONLY.  Imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker; the shipped library
-never imports it.
+TEST INFRASTRUCTURE ONLY.  Imported by ``tests/`` and
+``__graft_entry__.smoke()``, which compare the GPU results with it, and by the
+CPU-baseline leg of ``bench.py``, which times it; the shipped library never
+imports it.
 
 Parity status: the reference publishes no golden vectors and cannot run here
 (it is Julia), so the oracle is pinned by physical known-answer tests -- strictly
