@@ -36,6 +36,23 @@ def test_block_partition_covers_the_matrix_once():
     assert nadm > 0
 
 
+def test_touching_boxes_and_repeated_centres_are_never_admissible():
+    """Blocks whose boxes touch (distance 0) stay dense even when both boxes
+    are points: a single element, and clusters of identical centres."""
+    from qdfn.hmatrix import ClusterTree, block_partition, host_partition
+    perm, spans = host_partition(np.array([[1.0, 2.0, 3.0]]), leaf=8)
+    assert spans == [(0, 1, 0, 1, False)]
+    pts = np.repeat(np.array([[0.0, 0.0, 0.0], [5000.0, 0.0, 0.0]]), 20, axis=0)
+    t = ClusterTree(pts, leaf=4)
+    for s, r, adm in block_partition(t, eta=2.0):
+        if adm:
+            assert t.dist(s, r) > 0
+        else:
+            assert t.ends[s] - t.starts[s] <= 4 and t.ends[r] - t.starts[r] <= 4
+    # the two clusters, 5 km apart and each a point, are low-rank to each other
+    assert any(adm for _, _, adm in block_partition(t, eta=2.0))
+
+
 @pytest.mark.gpu
 def test_hmatrix_operator_matches_dense_and_oracle(qdfn_mod, oracle_mod):
     from qdfn import assemble, hmatrix, simulate, synth
