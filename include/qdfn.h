@@ -213,12 +213,14 @@ int qdfn_sync(qdfn_ctx* ctx);
 int qdfn_kernels_per_run(const qdfn_ctx* ctx);
 
 /* Cap the thread blocks (one per SM) a context's runs use; 0 = every SM
- * (default).  Contexts whose caps add up to at most the SM count run side by
- * side when launched with qdfn_run_async on different streams -- a batched
- * ensemble of geometries of uneven size, each on its share of the GPU.  The
- * operator tiling is re-sized for the cap.  qdfn_get_blocks returns the block
- * count of the next run (-1 for a null context).  No counterpart in the
- * reference, which runs one geometry per process. */
+ * (default).  The operator tiling is re-sized for the cap.  To run several
+ * contexts at once, group them in an ensemble (qdfn_ensemble_*, below): one
+ * cooperative launch holds every member, so their blocks are co-resident;
+ * separate cooperative launches on different streams carry no such guarantee,
+ * and a member whose blocks are not all resident waits at its grid barrier
+ * until its time budget ends the run.  qdfn_get_blocks returns the block count
+ * of the next run (-1 for a null context).  No counterpart in the reference,
+ * which runs one geometry per process. */
 int qdfn_set_blocks(qdfn_ctx* ctx, int nblocks);
 int qdfn_get_blocks(const qdfn_ctx* ctx);
 
