@@ -265,7 +265,10 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     // partition by frontier rounds; buffers grow and the round is redone when a count overflows
     std::vector<int4> blocks;
     {
-        unsigned cap_f = 1u << 16, cap_b = (unsigned)std::min<int64_t>((int64_t)1 << 30, 64 * (int64_t)nn + 1024);
+        // small first buffers, doubled on demand (a round that overflows is
+        // redone): every partition of more than 1024 blocks or frontier pairs
+        // goes through the growth path, so the tests exercise it
+        unsigned cap_f = 1024u, cap_b = 1024u;
         DBuf<int2> fa, fb;
         DBuf<int4> db;
         DBuf<unsigned> dcnt;   // [0] next frontier, [1] blocks
