@@ -855,6 +855,19 @@ def run_ensemble(args):
     solves = sum(c1["lowv_solves"] + c1["highv_solves"] - c0["lowv_solves"] - c0["highv_solves"]
                  for c0, c1 in zip(cnt0, cnt))
     fp64_tf = fp64_peak_tflops(dev) if rank == 0 else None
+    # the unit the ensemble is bound by: FP64 instructions of the friction
+    # solves per second (the committed capture's instructions per patch solve
+    # x the window's solves per second) against the measured FP64 rate (one
+    # DFMA per two flops of the FP64 GEMM)
+    fp64_pipe = None
+    if prof and prof.get("fp64_warp_inst_per_patch_solve") and fp64_tf:
+        inst = solves / max(ms / 1e3, 1e-9) * 32.0 * float(prof["fp64_warp_inst_per_patch_solve"])
+        fp64_pipe = {"achieved": inst / 1e12, "peak": fp64_tf / 2.0, "unit": "T FP64 lane-instructions/s",
+                     "frac": inst / 1e12 / (fp64_tf / 2.0),
+                     "note": "patch solves/s x %.1f FP64 warp instructions per solve (ncu, "
+                             "profiles/k_sim_members_c4_fp32.md) x 32 lanes, against half the measured FP64 "
+                             "GEMM flop rate; ncu: FP64 pipe %.1f %% busy over the captured launch"
+                             % (float(prof["fp64_warp_inst_per_patch_solve"]), float(prof.get("fp64_pipe_active_pct", 0)))}
 
     def fill_window(e, snap):
         """The same window in fill mode: members that have taken K steps keep
@@ -980,6 +993,7 @@ def run_ensemble(args):
                                  "the DRAM/algorithmic ratio of the committed ncu capture of a smaller ensemble of "
                                  "the same generator (profiles/k_sim_members_c4_fp32.md)"
                                  % (esz, peak_kind, solves / max(ms / 1e3, 1e-9))},
+            "fp64_pipe": fp64_pipe,
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
             "fill_mode": dict(fill, note="the same window with members that have taken K steps stepping on "
