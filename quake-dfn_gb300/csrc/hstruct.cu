@@ -189,9 +189,9 @@ extern "C" int qdfn_hstruct_build(qdfn_hstruct** out, int64_t N, const double* c
     if (N < 1 || N > (int64_t)1 << 30) return fail(QDFN_ERR_INVALID, "N must be in 1..2^30");
     if (leaf < 1) return fail(QDFN_ERR_INVALID, "leaf must be >= 1");
     if (!(eta > 0) || !std::isfinite(eta)) return fail(QDFN_ERR_INVALID, "eta must be positive");
+    if (N / leaf > ((int64_t)1 << 27)) return fail(QDFN_ERR_INVALID, "too many tree nodes (raise leaf)");
     for (int64_t i = 0; i < 3 * N; ++i)
         if (!std::isfinite(centres[i])) return fail(QDFN_ERR_INVALID, "centres must be finite");
-    if (N / leaf > ((int64_t)1 << 27)) return fail(QDFN_ERR_INVALID, "too many tree nodes (raise leaf)");
     // the tree's shape depends on N and leaf only: level order, halving
     std::vector<long long> nstart{0}, nend{N};
     std::vector<int2> child;

@@ -52,6 +52,38 @@ def test_invalid_arguments_are_rejected_on_the_host(qdfn_mod):
     assert rc == -15
 
 
+def test_new_entry_points_reject_bad_arguments_on_the_host(qdfn_mod):
+    """The H-structure, ensemble-state and early-column calls check their
+    arguments before any device work (no GPU needed)."""
+    import ctypes as C
+    import numpy as np
+    from qdfn import _lib
+    L = _lib.load()
+    h = C.c_void_p()
+    c = np.zeros((4, 3))
+    assert L.qdfn_hstruct_build(None, 4, C.c_void_p(c.ctypes.data), 8, 2.0) == -1
+    assert L.qdfn_hstruct_build(C.byref(h), 0, C.c_void_p(c.ctypes.data), 8, 2.0) == -1
+    assert L.qdfn_hstruct_build(C.byref(h), 4, C.c_void_p(c.ctypes.data), 0, 2.0) == -1
+    assert "leaf" in _lib.last_error()
+    assert L.qdfn_hstruct_build(C.byref(h), 4, C.c_void_p(c.ctypes.data), 8, -1.0) == -1
+    assert L.qdfn_hstruct_build(C.byref(h), 4, C.c_void_p(c.ctypes.data), 8, float("nan")) == -1
+    bad = c.copy()
+    bad[2, 1] = np.inf
+    assert L.qdfn_hstruct_build(C.byref(h), 4, C.c_void_p(bad.ctypes.data), 8, 2.0) == -1
+    assert "finite" in _lib.last_error()
+    assert L.qdfn_hstruct_build(C.byref(h), 1 << 30, C.c_void_p(c.ctypes.data), 1, 2.0) == -1
+    assert "tree nodes" in _lib.last_error()
+    assert L.qdfn_hstruct_sizes(None, None, None) == -1
+    assert L.qdfn_hstruct_get(None, None, None, None) == -1
+    assert L.qdfn_hstruct_destroy(None) == 0
+    n = C.c_int64()
+    assert L.qdfn_ensemble_state_bytes(None, C.byref(n)) == -1
+    assert L.qdfn_ensemble_set_state_all(None, C.c_void_p(c.ctypes.data), None) == -1
+    assert L.qdfn_ensemble_get_state_all(None, C.c_void_p(c.ctypes.data), None, 1) == -1
+    assert L.qdfn_set_early_cols(None, 4) == -1
+    assert L.qdfn_get_early_cols(None) == -1
+
+
 def test_context_rejects_bad_problems(qdfn_mod):
     import ctypes as C
     import numpy as np
